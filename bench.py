@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Benchmark: Richardson-Lucy voxel-iterations/s on the stage-scan light-sheet
+workload (101x256x512 uint16 raw at 31.5 deg, dz 0.3 um, dxy 0.104 um ->
+deskew to 100x256x756, 15 Biggs-Andrews RL iterations, rotate to
+150x256x723), synthetic seeded data.
+
+One step = one full pass of the hot path over the stack: crop, background
+subtraction, deskew, 15 RL iterations, rotation.
+
+  value : inputs already resident in HBM, cdx_RL_device on a stream, timed
+          with CUDA events (device time), voxel-iterations/s of the decon grid
+  e2e   : RL_interface (the reference's C entry point) with pinned host
+          buffers, host<->device copies inside the timed region
+  roofline : one RL iteration against the measured HBM copy bandwidth, with
+          56 B of algorithmic traffic per voxel-iteration, timed per pass with
+          CUDA events recorded by the library on its launch stream
+  cpu_baseline : the CPU restatement (scipy.fft float32, all host cores) on
+          a bounded sample (2 of the 15 iterations) of the same volume
+
+--impl reference times the reference path on the host CPU.  The reference
+has no CPU implementation of this loop (its RL runs only through cuFFT on a
+GPU), so the timed CPU arm is the restatement of that loop in oracle/.
+
+Multi-GPU: independent stacks do not exchange data, so N ranks run N
+replicas (weak scaling); value is the work of all ranks over the slowest
+rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ALG_BYTES_PER_VOXEL_ITER = 56.0  # one fused iteration, float32 storage
+
+WORKLOAD = dict(
+    name="stage-scan light-sheet 101x256x512 u16, deskew 31.5deg -> 100x256x756, 15 RL it, rotate",
+    raw_shape=(101, 256, 512), dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.2, angle=31.5,
+    background=100.0, n_iters=15, otf_nr=129, otf_nz=64, psf_sigma_xy=1.3, psf_sigma_z=3.0,
+    seed=1002,
+)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_inputs(tmpdir):
+    from cudadecon_gb300 import synth
+    w = WORKLOAD
+    raw = synth.bead_stack(w["raw_shape"], n_beads=300, sigma_range=(0.5, 2.0),
+                           amp_range=(500.0, 5000.0), psf_sigma_xy=w["psf_sigma_xy"],
+                           psf_sigma_z=w["psf_sigma_z"], background=w["background"],
+                           n_filaments=12, seed=w["seed"])
+    tab = synth.gaussian_otf_table(w["otf_nr"], w["otf_nz"], w["psf_sigma_xy"], w["psf_sigma_z"])
+    otf_path = Path(tmpdir) / "otf.tif"
+    synth.write_otf(otf_path, tab)
+    return raw, tab, otf_path
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index):
+        self.dev = dev_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_prepare(raw, tab):
+    """CPU-baseline leg: the oracle's deskewed start volume and OTF grid."""
+    from oracle import rl_oracle as O
+    from cudadecon_gb300 import synth
+    w = WORKLOAD
+    nz, ny, nx = w["raw_shape"]
+    st = O.rl_init(nx, ny, nz, w["dr"], w["dz"], w["dr_psf"], w["dz_psf"], w["angle"], w["angle"],
+                   0, False, synth.otf_table_to_image(tab))
+    X = raw[:st.output_nz, :st.output_ny, :st.output_nx].astype(np.float32)
+    X = O.bgsub(X, w["background"])
+    X = O.deskew(X, st.deskewFactor, st.deskewedXdim)
+    H = O.otf_on_grid(st, st.deskewedXdim, st.output_ny, st.output_nz)
+    return X, H
+
+
+def cpu_time_iterations(X, H, n_iters, workers):
+    """Time n_iters float32 RL iterations of the oracle: (voxel-iter/s, seconds)."""
+    from oracle import rl_oracle as O
+    t0 = time.perf_counter()
+    O.rl_iterations(X, X, H, n_iters, workers=workers)
+    dt = time.perf_counter() - t0
+    return X.size * n_iters / dt, dt
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        if pg:
+            pg.barrier()
+        return 0
+    with tempfile.TemporaryDirectory() as td:
+        raw, tab, _ = make_inputs(td)
+    cores = os.cpu_count() or 1
+    sample_iters = 1
+    X, H = cpu_prepare(raw, tab)
+    nvox = X.size
+    for _ in range(args.warmup):
+        cpu_time_iterations(X, H, 1, cores)
+    vals = [cpu_time_iterations(X, H, sample_iters, cores)[0] for _ in range(args.steps)]
+    v = statistics.median(vals)
+    sample = (f"{sample_iters} of {WORKLOAD['n_iters']} RL iterations per step on the deskewed "
+              f"{nvox}-voxel volume (scipy.fft float32, {cores} threads)")
+    line = {
+        "impl": "reference", "metric": "RL voxel-iterations/s", "value": v,
+        "unit": "voxel-iter/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * nvox * sample_iters / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD["name"], "l2_policy": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    import cudadecon_gb300 as cdx
+    L = cdx.lib()
+    w = WORKLOAD
+    nz, ny, nx = w["raw_shape"]
+    td = tempfile.TemporaryDirectory()
+    raw, tab, otf_path = make_inputs(td.name)
+    cdx.rl_init(w["raw_shape"], otf_path, dr=w["dr"], dz=w["dz"], dr_psf=w["dr_psf"],
+                dz_psf=w["dz_psf"], deskew_angle=w["angle"], rotation_angle=w["angle"])
+    onz, ony, onx = cdx.output_shape()
+    gz, gy, gx = cdx.decon_grid()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    d_raw = torch.from_numpy(raw).to(dev)
+    d_out = torch.empty((onz, ony, onx), dtype=torch.float32, device=dev)
+    n_iters = w["n_iters"]
+
+    def step():
+        ok = L.cdx_RL_device(ctypes.c_void_p(d_raw.data_ptr()), nx, ny, nz,
+                             ctypes.c_void_p(d_out.data_ptr()), None, w["background"], False,
+                             False, n_iters, 0, 0, 0, 0.0, False, False, sp)
+        if ok != 1:
+            raise RuntimeError(L.cdx_last_error().decode())
+
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    launches_per_step = int(L.cdx_last_launch_count())
+    grid_vox = gz * gy * gx
+    # ---- timed region (device-resident inputs)
+    clk = ClockSampler(local)
+    clk.start()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    if pg:
+        import torch.distributed as dist
+        t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_per_step = dev_ms / args.steps
+    vox_iters = grid_vox * n_iters
+    value = world * vox_iters / (ms_per_step / 1000.0)
+    finite = bool(torch.isfinite(d_out).all().item())
+
+    # ---- per-pass timing of the iteration (CUDA events on the library's launch stream)
+    L.cdx_profile_enable(1)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            step()
+    stream.synchronize()
+    pm = (ctypes.c_double * 9)()
+    pn = (ctypes.c_longlong * 9)()
+    it_ms = ctypes.c_double(0)
+    it_n = ctypes.c_longlong(0)
+    L.cdx_profile_read(pm, pn, 9, ctypes.byref(it_ms), ctypes.byref(it_n))
+    L.cdx_profile_enable(0)
+    iter_ms = it_ms.value / max(it_n.value, 1)
+    pass_bytes = [12, 8, 8, 8, 12, 8, 8, 8, 24]  # bytes per voxel moved by each pass as built
+    passes = {}
+    for i in range(9):
+        ms = pm[i] / max(pn[i], 1)
+        passes[L.cdx_profile_pass_name(i).decode()] = {
+            "ms": round(ms, 5), "bytes_per_voxel": pass_bytes[i],
+            "gbs": round(pass_bytes[i] * grid_vox / (ms * 1e-3) / 1e9, 1) if ms > 0 else None}
+    hbm, peak_kind = peaks()
+    achieved = ALG_BYTES_PER_VOXEL_ITER * grid_vox / (iter_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic_rl_iteration_c2.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
+
+    # ---- e2e through the reference ABI with pinned host buffers
+    h_raw = torch.from_numpy(raw).pin_memory()
+    h_out = torch.empty((onz, ony, onx), dtype=torch.float32).pin_memory()
+    u16p = ctypes.POINTER(ctypes.c_ushort)
+    f32p = ctypes.POINTER(ctypes.c_float)
+    rawp = ctypes.cast(ctypes.c_void_p(h_raw.data_ptr()), u16p)
+    outp = ctypes.cast(ctypes.c_void_p(h_out.data_ptr()), f32p)
+
+    def e2e_step():
+        ok = L.RL_interface(rawp, nx, ny, nz, outp, None, w["background"], False, False, n_iters,
+                            0, 0, 0, 0.0, False, False)
+        if ok != 1:
+            raise RuntimeError(L.cdx_last_error().decode())
+
+    e2e_step()
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if pg:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = world * vox_iters / e2e_s
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        X, H = cpu_prepare(raw, tab)
+        cpu_time_iterations(X, H, 1, cores)  # warm-up (FFT plans, page faults)
+        v, dt = cpu_time_iterations(X, H, 2, cores)
+        nvox = X.size
+        cpu = {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+               "sample": f"2 of 15 RL iterations on the deskewed {nvox}-voxel volume "
+                         f"(scipy.fft float32, {cores} threads), {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "RL voxel-iterations/s", "value": value, "unit": "voxel-iter/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded beads + filaments)",
+            "config": {"workload": WORKLOAD["name"], "decon_grid_zyx": [gz, gy, gx],
+                       "iterations": n_iters, "form": "plain FP32",
+                       "parallelism": f"replicas x{world}",
+                       "l2_policy": "working set ~0.45 GB > 129 MB L2 (no flush needed)"},
+            "e2e": {"value": e2e_val, "unit": "voxel-iter/s",
+                    "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": int(h_out.numel() * 4)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic,
+                         "kernel": "one RL iteration (9 fused passes)",
+                         "alg_bytes_per_voxel_iter": ALG_BYTES_PER_VOXEL_ITER,
+                         "iteration_ms": iter_ms, "peak_source": f"{peak_kind} hbm_gbs",
+                         "passes": passes},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+            "output_finite": finite,
+        }
+        print(json.dumps(line), flush=True)
+    td.cleanup()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

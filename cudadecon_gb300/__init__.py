@@ -1,0 +1,257 @@
+"""cudadecon_gb300: GB300-native Richardson-Lucy deconvolution with the cudaDecon C ABI.
+
+The product is the in-tree shared library ``lib/libcudaDecon.so`` (CUDA for
+sm_103a plus C++ host code).  This module binds it with ctypes the way a
+pycudadecon-style caller binds the reference library, and adds numpy helpers.
+There is no CPU fallback: every function raises if the library is missing.
+
+Reference ABI: scopetools/cudadecon src/linearDecon.h:243-317.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_bool, c_char_p, c_double, c_float, c_int, c_longlong, c_size_t
+from ctypes import c_uint, c_ushort, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+__all__ = [
+    "lib",
+    "build",
+    "lib_path",
+    "CudaDeconError",
+    "rl_init",
+    "rl_decon",
+    "rl_cleanup",
+    "output_shape",
+    "deskew",
+    "affine",
+    "affine_ra",
+    "camcor_init",
+    "camcor",
+    "load_image",
+]
+
+_LIB = None
+
+
+class CudaDeconError(RuntimeError):
+    """A library entry point returned failure (the message is cdx_last_error())."""
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile the CUDA library in-tree for sm_103a (nvcc required)."""
+    global _LIB
+    p = _build.build(verbose=verbose, force=force)
+    return p
+
+
+_F = POINTER(c_float)
+_U16 = POINTER(c_ushort)
+
+
+def _bind(L) -> None:
+    sig = {
+        # reference ABI (src/linearDecon.h:260-316)
+        "RL_interface_init": (c_int, [c_int, c_int, c_int, c_float, c_float, c_float, c_float,
+                                      c_float, c_float, c_int, c_bool, c_char_p]),
+        "RL_interface": (c_int, [_U16, c_int, c_int, c_int, _F, _F, c_float, c_bool, c_bool,
+                                 c_int, c_int, c_int, c_int, c_float, c_bool, c_bool]),
+        "Deskew_interface": (c_int, [_F, c_int, c_int, c_int, c_float, c_float, c_float, _F,
+                                     c_int, c_int, c_float]),
+        "Affine_interface": (c_int, [_F, c_int, c_int, c_int, _F, _F]),
+        "Affine_interface_RA": (c_int, [_F, c_int, c_int, c_int, c_float, c_float, c_float,
+                                        _F, _F]),
+        "camcor_interface_init": (c_int, [c_int, c_int, c_int, _F]),
+        "camcor_interface": (c_int, [_U16, c_int, c_int, c_int, _U16]),
+        "RL_cleanup": (None, []),
+        "cuda_reset": (None, []),
+        "get_output_nx": (c_uint, []),
+        "get_output_ny": (c_uint, []),
+        "get_output_nz": (c_uint, []),
+        "get_version": (c_char_p, []),
+        # extensions
+        "cdx_last_error": (c_char_p, []),
+        "cdx_RL_device": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_float,
+                                  c_bool, c_bool, c_int, c_int, c_int, c_int, c_float, c_bool,
+                                  c_bool, c_void_p]),
+        "cdx_last_launch_count": (c_longlong, []),
+        "cdx_decon_grid": (c_int, [POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
+        "cdx_profile_enable": (c_int, [c_int]),
+        "cdx_profile_read": (c_int, [POINTER(c_double), POINTER(c_longlong), c_int,
+                                     POINTER(c_double), POINTER(c_longlong)]),
+        "cdx_profile_pass_name": (c_char_p, [c_int]),
+        "cdx_deskew_device": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_void_p, c_int,
+                                      c_int, c_float, c_void_p]),
+        "cdx_rotate_device": (c_int, [c_void_p, c_int, c_int, c_int, _F, c_void_p, c_int, c_int,
+                                      c_void_p]),
+        "cdx_camcor_device": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
+                                      c_void_p]),
+        "cdx_rfft3d_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
+        "cdx_conv3d_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+        "cdx_fft_length_supported": (c_int, [c_int]),
+        "cdx_load_image": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), POINTER(c_int), _F,
+                                   c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """The loaded library (ctypes.CDLL); raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        p = lib_path()
+        if not p.exists():
+            raise CudaDeconError(
+                f"{p} is missing: build it with cudadecon_gb300.build() "
+                "(or __graft_entry__.build()); there is no CPU fallback")
+        L = ctypes.CDLL(str(p), mode=os.RTLD_LOCAL if hasattr(os, "RTLD_LOCAL") else 0)
+        _bind(L)
+        _LIB = L
+    return _LIB
+
+
+def _err(what: str):
+    msg = lib().cdx_last_error()
+    raise CudaDeconError(f"{what} failed: {msg.decode() if msg else ''}")
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(_F)
+
+
+def _u16ptr(a: np.ndarray):
+    return a.ctypes.data_as(_U16)
+
+
+# ---------------------------------------------------------------- RL
+def rl_init(shape_zyx, otf_file, dr=0.104, dz=0.5, dr_psf=0.104, dz_psf=0.1, deskew_angle=0.0,
+            rotation_angle=0.0, output_width=0, skewed_decon=False) -> None:
+    """RL_interface_init for a raw stack of shape (nz, ny, nx)."""
+    nz, ny, nx = (int(v) for v in shape_zyx)
+    ok = lib().RL_interface_init(nx, ny, nz, dr, dz, dr_psf, dz_psf, deskew_angle,
+                                 rotation_angle, int(output_width), bool(skewed_decon),
+                                 str(otf_file).encode())
+    if ok != 1:
+        _err("RL_interface_init")
+
+
+def decon_grid():
+    """(nz, ny, nx) of the grid the RL iterations run on after the last rl_init."""
+    x, y, z = c_int(0), c_int(0), c_int(0)
+    if lib().cdx_decon_grid(ctypes.byref(x), ctypes.byref(y), ctypes.byref(z)) != 1:
+        _err("cdx_decon_grid")
+    return z.value, y.value, x.value
+
+
+def output_shape():
+    """(nz, ny, nx) of the RL_interface result after the last rl_init."""
+    L = lib()
+    return int(L.get_output_nz()), int(L.get_output_ny()), int(L.get_output_nx())
+
+
+def rl_decon(raw: np.ndarray, background=100.0, n_iters=10, rescale=False, save_deskewed=False,
+             extra_shift=0, napodize=0, nzblend=0, pad_val=0.0, dup_rev_stack=False,
+             skewed_decon=False, deskewed_shape=None):
+    """RL_interface on a (nz, ny, nx) uint16 stack; returns the float32 result
+    (and the deskewed raw stack when save_deskewed)."""
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    nz, ny, nx = raw.shape
+    out = np.zeros(output_shape(), dtype=np.float32)
+    desk = None
+    if save_deskewed:
+        if deskewed_shape is None:
+            raise ValueError("deskewed_shape is required with save_deskewed")
+        desk = np.zeros(deskewed_shape, dtype=np.float32)
+    ok = lib().RL_interface(_u16ptr(raw), nx, ny, nz, _fptr(out),
+                            _fptr(desk) if desk is not None else None, background, bool(rescale),
+                            bool(save_deskewed), int(n_iters), int(extra_shift), int(napodize),
+                            int(nzblend), float(pad_val), bool(dup_rev_stack), bool(skewed_decon))
+    if ok != 1:
+        _err("RL_interface")
+    return (out, desk) if save_deskewed else out
+
+
+def rl_cleanup() -> None:
+    lib().RL_cleanup()
+
+
+# ---------------------------------------------------------------- geometry
+def deskew(stack: np.ndarray, angle, dz, dr, output_width=0, extra_shift=0, pad_val=0.0,
+           out_width=None):
+    """Deskew_interface on a (nz, ny, nx) float32 stack.  The output width is
+    output_width, or when 0 the reference's rule (see include/cudadecon.h);
+    pass out_width to size the result buffer for that rule."""
+    a = np.ascontiguousarray(stack, dtype=np.float32)
+    nz, ny, nx = a.shape
+    w = int(output_width) if output_width else int(out_width if out_width is not None else nx)
+    out = np.zeros((nz, ny, w), dtype=np.float32)
+    ok = lib().Deskew_interface(_fptr(a), nx, ny, nz, dz, dr, angle, _fptr(out),
+                                int(output_width), int(extra_shift), float(pad_val))
+    if ok != 1:
+        _err("Deskew_interface")
+    return out
+
+
+def affine(stack: np.ndarray, mat4x4) -> np.ndarray:
+    a = np.ascontiguousarray(stack, dtype=np.float32)
+    m = np.ascontiguousarray(mat4x4, dtype=np.float32).reshape(16)
+    nz, ny, nx = a.shape
+    out = np.zeros_like(a)
+    if lib().Affine_interface(_fptr(a), nx, ny, nz, _fptr(out), _fptr(m)) != 1:
+        _err("Affine_interface")
+    return out
+
+
+def affine_ra(stack: np.ndarray, mat4x4, dx, dy, dz) -> np.ndarray:
+    a = np.ascontiguousarray(stack, dtype=np.float32)
+    m = np.ascontiguousarray(mat4x4, dtype=np.float32).reshape(16)
+    nz, ny, nx = a.shape
+    out = np.zeros_like(a)
+    if lib().Affine_interface_RA(_fptr(a), nx, ny, nz, dx, dy, dz, _fptr(out), _fptr(m)) != 1:
+        _err("Affine_interface_RA")
+    return out
+
+
+def camcor_init(shape_zyx, camparam: np.ndarray) -> None:
+    """camcor_interface_init; camparam is (3, ny, nx) float32: a, b, offset."""
+    nz, ny, nx = (int(v) for v in shape_zyx)
+    p = np.ascontiguousarray(camparam, dtype=np.float32)
+    if p.shape != (3, ny, nx):
+        raise ValueError("camparam must have shape (3, ny, nx)")
+    if lib().camcor_interface_init(nx, ny, nz, _fptr(p)) != 1:
+        _err("camcor_interface_init")
+
+
+def camcor(raw: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(raw, dtype=np.uint16)
+    nz, ny, nx = a.shape
+    out = np.zeros_like(a)
+    if lib().camcor_interface(_u16ptr(a), nx, ny, nz, _u16ptr(out)) != 1:
+        _err("camcor_interface")
+    return out
+
+
+def load_image(path) -> np.ndarray:
+    """Read a TIFF / .cimg file as the library reads OTFs; returns (d, h, w) float32."""
+    L = lib()
+    w, h, d = c_int(0), c_int(0), c_int(0)
+    if L.cdx_load_image(str(path).encode(), ctypes.byref(w), ctypes.byref(h), ctypes.byref(d),
+                        None, 0) != 1:
+        _err("cdx_load_image")
+    out = np.zeros((d.value, h.value, w.value), dtype=np.float32)
+    if L.cdx_load_image(str(path).encode(), None, None, None, _fptr(out), out.size) != 1:
+        _err("cdx_load_image")
+    return out

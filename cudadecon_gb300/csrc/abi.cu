@@ -1,0 +1,982 @@
+// C ABI and host orchestration.
+//
+// Session state mirrors the reference library's globals
+// (src/RL-Biggs-Andrews.cpp:459-466 and the bleach statics at :46-47): the
+// output sizes, deskew factor and width, rotation matrix and OTF survive from
+// RL_interface_init until RL_cleanup.  Device work buffers, FFT twiddle
+// tables and OTF tables are allocated once per decon grid and reused across
+// RL_interface calls (the reference allocates and frees them on every call).
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cudadecon.h"
+#include "kernels.h"
+#include "otf_io.h"
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+namespace cdx {
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_err;
+static std::string g_err_shared;
+static std::mutex g_err_mu;
+
+void set_error(const char* where, const char* what) {
+  std::string s = std::string(where) + ": " + what;
+  g_err = s;
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err_shared = s;
+}
+
+void set_cuda_error(const char* where, cudaError_t err) { set_error(where, cudaGetErrorString(err)); }
+
+// ---------------------------------------------------------------- sizes
+// Good FFT sizes are products of 2, 3, 5 and 7 (notGoodDimension /
+// findOptimalDimension, src/RL-Biggs-Andrews.cpp:18-43).  Sizes below 2 have
+// no good size below them (the reference recurses forever); 0 is returned.
+static bool not_good_dimension(unsigned num) {
+  if (num == 2 || num == 3 || num == 5 || num == 7) return false;
+  if (num < 2) return true;
+  if (num % 2 == 0) return not_good_dimension(num / 2);
+  if (num % 3 == 0) return not_good_dimension(num / 3);
+  if (num % 5 == 0) return not_good_dimension(num / 5);
+  if (num % 7 == 0) return not_good_dimension(num / 7);
+  return true;
+}
+
+static unsigned find_optimal_dimension(unsigned in, int step = -1) {
+  unsigned out = in;
+  while (out >= 2 && not_good_dimension(out)) out += step;
+  return out >= 2 ? out : 0;
+}
+
+// ---------------------------------------------------------------- device buffers
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  int ensure(size_t count) {
+    if (count <= n && p) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (count == 0) return 0;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_cuda_error("cudaMalloc", e);
+      return e;
+    }
+    n = count;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// FFT plans and OTF table for one decon grid.
+struct GridPlan {
+  bool valid = false;
+  Geom g{};
+  FftLen fx, fy, fz;
+  OtfDev otf{};
+  DevBuf<float2> tz, full;
+  void release() {
+    fft_len_free(fx);
+    fft_len_free(fy);
+    fft_len_free(fz);
+    tz.release();
+    full.release();
+    valid = false;
+  }
+};
+
+struct Session {
+  // values set by RL_interface_init (reference globals)
+  bool inited = false;
+  unsigned output_nx = 0, output_ny = 0, output_nz = 0;
+  bool bCrop = false;
+  double deskewFactor = 0.0;
+  unsigned deskewedXdim = 0;
+  bool has_rot = false;
+  float rot[4] = {0, 0, 0, 0};
+  float dr = 0, dz = 0;  // dz after the deskew update
+  float dkx_otf = 0, dky_otf = 0, dkz_otf = 0;
+  RawOtfDims od{};
+  DevBuf<float2> raw_otf;
+  // bleach correction statics (RL-Biggs-Andrews.cpp:46-47)
+  double intensity_overall0 = 0.0;
+  bool bFirstTime = true;
+  // work buffers
+  GridPlan plan;
+  DevBuf<unsigned short> u16in;
+  DevBuf<float> pre, Xa, Xb, G, raw, rotbuf, res_stage, desk_stage, conv_tmp;
+  DevBuf<float2> S;
+  DevBuf<double> partials, stat_d;
+  DevBuf<unsigned> counter, stat_u;
+  DevBuf<float> lam;
+  cudaStream_t stream = nullptr;
+  long long launches = 0;
+  // camcor context
+  int cc_nx = 0, cc_ny = 0, cc_nz = 0;
+  DevBuf<float> cc_param;
+  DevBuf<unsigned short> cc_in, cc_out;
+};
+
+static Session g_s;
+static std::mutex g_mu;
+
+// Optional per-pass timing with CUDA events recorded on the launch stream
+// (cdx_profile_enable / cdx_profile_read).  Pass p of an iteration is timed
+// between the events before and after its launch.
+constexpr int kPasses = 9;
+static const char* kPassNames[kPasses] = {"x_fwd_predict", "y_fwd",       "z_otf",
+                                          "y_inv",         "x_ratio_fwd", "y_fwd2",
+                                          "z_otf_conj",    "y_inv2",      "x_inv_update"};
+struct Profiler {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;  // 10 events per recorded iteration
+  int used = 0;
+  double pass_ms[kPasses] = {0};
+  long long pass_n[kPasses] = {0};
+  double iter_ms = 0;
+  long long iter_n = 0;
+};
+static Profiler g_prof;
+
+static cudaEvent_t prof_event() {
+  Profiler& P = g_prof;
+  if (P.used == (int)P.ev.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    P.ev.push_back(e);
+  }
+  return P.ev[P.used++];
+}
+
+// Fold the recorded events into the accumulators (synchronises).
+static void prof_collect() {
+  Profiler& P = g_prof;
+  if (P.used < 10) {
+    P.used = 0;
+    return;
+  }
+  cudaEventSynchronize(P.ev[P.used - 1]);
+  for (int base = 0; base + 10 <= P.used; base += 10) {
+    for (int p = 0; p < kPasses; ++p) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, P.ev[base + p], P.ev[base + p + 1]) == cudaSuccess) {
+        P.pass_ms[p] += ms;
+        P.pass_n[p] += 1;
+      }
+    }
+    float it = 0.f;
+    if (cudaEventElapsedTime(&it, P.ev[base], P.ev[base + kPasses]) == cudaSuccess) {
+      P.iter_ms += it;
+      P.iter_n += 1;
+    }
+  }
+  P.used = 0;
+}
+
+static void release_all(Session& s) {
+  s.plan.release();
+  s.raw_otf.release();
+  s.u16in.release();
+  s.pre.release();
+  s.Xa.release();
+  s.Xb.release();
+  s.G.release();
+  s.raw.release();
+  s.rotbuf.release();
+  s.res_stage.release();
+  s.desk_stage.release();
+  s.conv_tmp.release();
+  s.S.release();
+  s.partials.release();
+  s.stat_d.release();
+  s.counter.release();
+  s.stat_u.release();
+  s.lam.release();
+  s.cc_param.release();
+  s.cc_in.release();
+  s.cc_out.release();
+  if (s.stream) cudaStreamDestroy(s.stream);
+  s.stream = nullptr;
+}
+
+static int ensure_stream(Session& s) {
+  if (!s.stream) CDX_CHECK(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+  return 0;
+}
+
+// Build (or reuse) FFT plans and the OTF table for a decon grid (gx, gy, gz).
+// The OTF k-scales follow RL_interface_init (RL-Biggs-Andrews.cpp:634-642):
+// dk = 1/(pixel * size) per axis divided by the OTF's dk.
+static int ensure_plan(Session& s, int gx, int gy, int gz) {
+  GridPlan& p = s.plan;
+  if (p.valid && p.g.nx == gx && p.g.ny == gy && p.g.nz == gz) return 0;
+  p.release();
+  if (!fft_len_supported(gx) || !fft_len_supported(gy) || !fft_len_supported(gz)) {
+    set_error("plan", "decon grid size is not a product of 2, 3, 5 and 7");
+    return cudaErrorInvalidValue;
+  }
+  p.g = make_geom(gx, gy, gz);
+  int rc;
+  if ((rc = fft_len_init(p.fx, gx))) return rc;
+  if ((rc = fft_len_init(p.fy, gy))) return rc;
+  if ((rc = fft_len_init(p.fz, gz))) return rc;
+  const float dkx = 1.0 / (s.dr * (unsigned)gx);
+  const float dky = 1.0 / (s.dr * (unsigned)gy);
+  const float dkz = 1.0 / (s.dz * (unsigned)gz);
+  RawOtfDims od = s.od;
+  od.kxscale = dkx / s.dkx_otf;
+  od.kyscale = dky / s.dky_otf;
+  od.kzscale = dkz / s.dkz_otf;
+  const float scale = (float)(1.0 / ((double)gx * gy * gz));
+  p.otf.nr = od.nx_otf;
+  p.otf.kxscale = od.kxscale;
+  p.otf.kyscale = od.kyscale;
+  p.otf.tz = nullptr;
+  p.otf.full = nullptr;
+  if (od.ny_otf == 1) {
+    p.otf.mode = 0;
+    if ((rc = p.tz.ensure((size_t)od.nx_otf * gz))) return rc;
+    if ((rc = launch_otf_tz(p.g, s.raw_otf.p, od, p.tz.p, scale, s.stream))) return rc;
+    p.otf.tz = p.tz.p;
+  } else {
+    p.otf.mode = 1;
+    if ((rc = p.full.ensure((size_t)p.g.spec_elems()))) return rc;
+    if ((rc = launch_otf_full(p.g, s.raw_otf.p, od, p.full.p, scale, s.stream))) return rc;
+    p.otf.full = p.full.p;
+  }
+  CDX_CHECK(cudaStreamSynchronize(s.stream));
+  p.valid = true;
+  return 0;
+}
+
+static int ensure_grid_buffers(Session& s, const Geom& g) {
+  const size_t n = (size_t)g.nvox();
+  int rc;
+  if ((rc = s.Xa.ensure(n)) || (rc = s.Xb.ensure(n)) || (rc = s.G.ensure(n)) ||
+      (rc = s.raw.ensure(n)) || (rc = s.S.ensure((size_t)g.spec_elems())))
+    return rc;
+  const int nblk = x_pass_blocks(g);
+  if ((rc = s.partials.ensure(2 * (size_t)nblk)) || (rc = s.counter.ensure(1)) ||
+      (rc = s.lam.ensure(2)))
+    return rc;
+  CDX_CHECK(cudaMemsetAsync(s.counter.p, 0, sizeof(unsigned), s.stream));
+  CDX_CHECK(cudaMemsetAsync(s.lam.p, 0, 2 * sizeof(float), s.stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------- RL loop
+// The iteration loop of RichardsonLucy_GPU (RL-Biggs-Andrews.cpp:282-367) on
+// the grid of s.plan, starting from X0 in s.Xa with raw in s.raw.  Returns
+// the buffer that holds the final estimate.
+static int rl_iterations(Session& s, int nIter, float** final_x) {
+  const GridPlan& p = s.plan;
+  const Geom& g = p.g;
+  RLWork w;
+  w.partials = s.partials.p;
+  w.counter = s.counter.p;
+  w.lam = s.lam.p;
+  w.max_blocks = (int)(s.partials.n / 2);
+  const float eps = 1.1920928955078125e-07f;  // std::numeric_limits<float>::epsilon()
+  float* X = s.Xa.p;
+  float* Xm1 = s.Xb.p;
+  int rc;
+  const bool prof = g_prof.on;
+  auto mark = [&]() {
+    if (prof) {
+      cudaEvent_t e = prof_event();
+      if (e) cudaEventRecord(e, s.stream);
+    }
+  };
+  for (int k = 0; k < nIter; ++k) {
+    const int predict = k > 1;
+    float* lam_k = s.lam.p + (k & 1);
+    float* lam_n = s.lam.p + ((k + 1) & 1);
+    mark();
+    if ((rc = launch_x_fwd(g, p.fx, X, Xm1, lam_k, predict, s.S.p, s.stream))) return rc;
+    mark();
+    if ((rc = launch_y_pass(g, p.fy, s.S.p, false, s.stream))) return rc;
+    mark();
+    if ((rc = launch_z_pass(g, p.fz, s.S.p, p.otf, false, s.stream))) return rc;
+    mark();
+    if ((rc = launch_y_pass(g, p.fy, s.S.p, true, s.stream))) return rc;
+    mark();
+    if ((rc = launch_x_inv_ratio_fwd(g, p.fx, s.S.p, s.raw.p, eps, s.stream))) return rc;
+    mark();
+    if ((rc = launch_y_pass(g, p.fy, s.S.p, false, s.stream))) return rc;
+    mark();
+    if ((rc = launch_z_pass(g, p.fz, s.S.p, p.otf, true, s.stream))) return rc;
+    mark();
+    if ((rc = launch_y_pass(g, p.fy, s.S.p, true, s.stream))) return rc;
+    mark();
+    if ((rc = launch_x_inv_update(g, p.fx, s.S.p, X, Xm1, lam_k, predict, Xm1, s.G.p, k >= 1, w,
+                                  lam_n, eps, s.stream)))
+      return rc;
+    mark();
+    if (prof && g_prof.used >= 10 * 64) prof_collect();
+    s.launches += 9;
+    float* t = X;
+    X = Xm1;
+    Xm1 = t;
+  }
+  *final_x = X;
+  return 0;
+}
+
+struct RLArgs {
+  int nx, ny, nz;  // caller's raw sizes
+  float background;
+  bool bDoRescale, bSaveDeskewedRaw;
+  int nIters, extraShift, napodize, nZblend;
+  float padVal;
+  bool bDupRevStack, bSkewedDecon;
+};
+
+static void rot_out_dims(const Session& s, int nx, int nz, int* nx_r, int* nz_r) {
+  const float* p = s.rot;
+  // RichardsonLucy_GPU (RL-Biggs-Andrews.cpp:410-411)
+  *nz_r = (int)(nz * p[3] / p[0]);
+  *nx_r = (int)(nx * p[3] + nz * p[2] * p[2] / fabsf(p[1]));
+}
+
+// The body of RichardsonLucy_GPU (RL-Biggs-Andrews.cpp:56-450) on device
+// memory.  d_u16 holds the caller's (nx, ny, nz) raw stack.  On return
+// *out_ptr / *out_dims describe the device buffer with the result.
+static int rl_pipeline(Session& s, const unsigned short* d_u16, const RLArgs& a, float* d_deskewed,
+                       const float** out_ptr, int out_dims[3]) {
+  int rc;
+  const int nx0 = s.output_nx, ny = s.output_ny, nz0 = s.output_nz;
+  if (a.nx < nx0 || a.ny < ny || a.nz < nz0) {
+    set_error("RL_interface", "input stack smaller than the RL_interface_init sizes");
+    return cudaErrorInvalidValue;
+  }
+  const size_t n0 = (size_t)nx0 * ny * nz0;
+  if ((rc = s.pre.ensure(n0))) return rc;
+  const bool save_desk = a.bSaveDeskewedRaw && fabs(s.deskewFactor) > 0.0;
+  const bool pre = a.nIters > 0 || save_desk || s.has_rot;
+  const bool fuse_bg = pre && a.napodize <= 0;
+  if ((rc = launch_u16_to_f32_crop(d_u16, a.nx, a.ny, nx0, ny, nz0, s.pre.p, a.background,
+                                   fuse_bg ? 1 : 0, s.stream)))
+    return rc;
+  ++s.launches;
+  const float* cur = s.pre.p;
+  int nx = nx0, nz = nz0;
+  bool cur_is_x = false;  // whether cur already lives in Xa
+  if (pre) {
+    if (!fuse_bg) {
+      if ((rc = launch_apodize(s.pre.p, nx0, ny, nz0, a.napodize, s.stream))) return rc;
+      if ((rc = launch_bgsub(s.pre.p, (long long)n0, a.background, s.stream))) return rc;
+      s.launches += 3;
+    }
+    if (a.bDoRescale) {
+      // meanAboveBackground_GPU + rescale (RL-Biggs-Andrews.cpp:124-134)
+      if ((rc = s.stat_d.ensure(1216 + 2)) || (rc = s.stat_u.ensure(1216 + 2))) return rc;
+      double intensity = 0.0;
+      if ((rc = mean_above_background(s.pre.p, (long long)n0, s.stat_d.p, s.stat_u.p, &intensity,
+                                      s.stream)))
+        return rc;
+      s.launches += 4;
+      if (s.bFirstTime) {
+        s.intensity_overall0 = intensity;
+        s.bFirstTime = false;
+      } else {
+        const float ratio = s.intensity_overall0 / intensity;
+        if ((rc = launch_scale(s.pre.p, (long long)n0, (double)ratio, s.stream))) return rc;
+        ++s.launches;
+      }
+    }
+    const bool deskew_now =
+        (!a.bSkewedDecon || (save_desk && a.nIters == 0)) && fabs(s.deskewFactor) > 0.0;
+    if (deskew_now) {
+      nx = s.deskewedXdim;
+      const size_t nd = (size_t)nx * ny * nz0;
+      if ((rc = s.Xa.ensure(nd))) return rc;
+      if ((rc = launch_deskew(s.pre.p, nx0, ny, nz0, s.deskewFactor, s.Xa.p, nx, a.extraShift,
+                              a.padVal, s.stream)))
+        return rc;
+      ++s.launches;
+      cur = s.Xa.p;
+      cur_is_x = true;
+      if (save_desk && d_deskewed)
+        CDX_CHECK(cudaMemcpyAsync(d_deskewed, cur, nd * sizeof(float), cudaMemcpyDeviceToDevice,
+                                  s.stream));
+      if (save_desk && a.nIters == 0) {
+        // The reference returns an unfilled buffer here; the deskewed stack is
+        // returned instead.
+        *out_ptr = cur;
+        out_dims[0] = nx;
+        out_dims[1] = ny;
+        out_dims[2] = nz;
+        return 0;
+      }
+    }
+    if (a.nZblend > 0) {
+      if (!cur_is_x) {
+        if ((rc = s.Xa.ensure(n0))) return rc;
+        CDX_CHECK(cudaMemcpyAsync(s.Xa.p, cur, n0 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                  s.stream));
+        cur = s.Xa.p;
+        cur_is_x = true;
+      }
+      if ((rc = launch_zblend(s.Xa.p, nx, ny, nz, a.nZblend, s.stream))) return rc;
+      ++s.launches;
+    }
+    if (a.bDupRevStack) {
+      // mirrored stack of 2*nz slices (RL-Biggs-Andrews.cpp:193-205); the FFT
+      // grid follows the doubled stack
+      const size_t nv = (size_t)nx * ny * nz;
+      if ((rc = s.raw.ensure(2 * nv))) return rc;
+      CDX_CHECK(cudaMemcpyAsync(s.raw.p, cur, nv * sizeof(float), cudaMemcpyDeviceToDevice,
+                                s.stream));
+      if ((rc = launch_dup_rev(s.raw.p, nx, ny, nz, s.stream))) return rc;
+      ++s.launches;
+      if ((rc = s.Xa.ensure(2 * nv))) return rc;
+      CDX_CHECK(cudaMemcpyAsync(s.Xa.p, s.raw.p, 2 * nv * sizeof(float), cudaMemcpyDeviceToDevice,
+                                s.stream));
+      cur = s.Xa.p;
+      cur_is_x = true;
+      nz *= 2;
+    }
+  }
+  const float* X = cur;
+  if (a.nIters > 0) {
+    if ((rc = ensure_plan(s, nx, ny, nz))) return rc;
+    if ((rc = ensure_grid_buffers(s, s.plan.g))) return rc;
+    const size_t nv = (size_t)nx * ny * nz;
+    if (cur != s.Xa.p)
+      CDX_CHECK(cudaMemcpyAsync(s.Xa.p, cur, nv * sizeof(float), cudaMemcpyDeviceToDevice, s.stream));
+    CDX_CHECK(cudaMemcpyAsync(s.raw.p, s.Xa.p, nv * sizeof(float), cudaMemcpyDeviceToDevice,
+                              s.stream));
+    float* fx = nullptr;
+    if ((rc = rl_iterations(s, a.nIters, &fx))) return rc;
+    X = fx;
+  }
+  if (a.bDupRevStack && pre) nz /= 2;
+  if (a.bSkewedDecon && fabs(s.deskewFactor) > 0.0) {
+    // deskew after decon (RL-Biggs-Andrews.cpp:383-401; padVal defaults to 0)
+    const int nxd = s.deskewedXdim;
+    if ((rc = s.desk_stage.ensure((size_t)nxd * ny * nz))) return rc;
+    if ((rc = launch_deskew(X, nx, ny, nz, s.deskewFactor, s.desk_stage.p, nxd, a.extraShift, 0.f,
+                            s.stream)))
+      return rc;
+    ++s.launches;
+    X = s.desk_stage.p;
+    nx = nxd;
+  }
+  if (s.has_rot) {
+    int nxr, nzr;
+    rot_out_dims(s, nx, nz, &nxr, &nzr);
+    if (nxr <= 0 || nzr <= 0) {
+      set_error("RL_interface", "rotation gives an empty output");
+      return cudaErrorInvalidValue;
+    }
+    if ((rc = s.rotbuf.ensure((size_t)nxr * ny * nzr))) return rc;
+    if ((rc = launch_rotate(X, nx, ny, nz, s.rot, s.rotbuf.p, nxr, nzr, s.stream))) return rc;
+    ++s.launches;
+    X = s.rotbuf.p;
+    nx = nxr;
+    nz = nzr;
+  }
+  *out_ptr = X;
+  out_dims[0] = nx;
+  out_dims[1] = ny;
+  out_dims[2] = nz;
+  return 0;
+}
+
+static unsigned reported_nx(const Session& s) {
+  if (s.has_rot) {
+    const float* p = s.rot;
+    int nx_afterRot = s.deskewedXdim * p[3] + s.output_nz * p[2] * p[2] / p[1];
+    return nx_afterRot;
+  }
+  return s.deskewedXdim;
+}
+
+static unsigned reported_nz(const Session& s) {
+  if (s.has_rot) {
+    const float* p = s.rot;
+    int nz_afterRot = s.output_nz * p[3] / p[0];
+    return nz_afterRot;
+  }
+  return s.output_nz;
+}
+
+static int init_session(Session& s, int nx, int ny, int nz, float dr, float dz, float dr_psf,
+                        float dz_psf, float deskewAngle, float rotationAngle, int outputWidth,
+                        bool bSkewedDecon, const char* otf_file) {
+  s.plan.release();
+  s.inited = false;
+  if (nx < 2 || ny < 2 || nz < 2) {
+    set_error("RL_interface_init", "image sizes must be at least 2");
+    return cudaErrorInvalidValue;
+  }
+  // RL-Biggs-Andrews.cpp:543-564
+  s.bCrop = false;
+  s.output_ny = find_optimal_dimension(ny);
+  if (s.output_ny != (unsigned)ny) s.bCrop = true;
+  s.output_nz = find_optimal_dimension(nz);
+  if (s.output_nz != (unsigned)nz) s.bCrop = true;
+  s.output_nx = nx;
+  if (!(fabs(deskewAngle) > 0.0)) {
+    s.output_nx = find_optimal_dimension(nx);
+    if (s.output_nx != (unsigned)nx) s.bCrop = true;
+  }
+  // OTF (RL-Biggs-Andrews.cpp:566-590)
+  HostImage otf;
+  std::string err;
+  if (!load_image_file(otf_file, otf, err)) {
+    set_error("RL_interface_init: OTF", err.c_str());
+    return cudaErrorInvalidValue;
+  }
+  if (bSkewedDecon) dz_psf *= fabs(sin(deskewAngle * M_PI / 180.));
+  // determine_OTF_dimensions (RL-Biggs-Andrews.cpp:506-529)
+  unsigned nx_otf, ny_otf, nz_otf;
+  if (otf.d > 1) {
+    nx_otf = otf.w / 2;
+    ny_otf = otf.h;
+    nz_otf = otf.d;
+  } else {
+    nx_otf = otf.h;
+    ny_otf = 1;
+    nz_otf = otf.w / 2;
+  }
+  if (nx_otf < 2 || nz_otf < 1) {
+    set_error("RL_interface_init", "OTF too small");
+    return cudaErrorInvalidValue;
+  }
+  s.dkx_otf = 1 / ((nx_otf - 1) * 2 * dr_psf);
+  s.dky_otf = ny_otf > 1 ? 1 / (ny_otf * dr_psf) : s.dkx_otf;
+  s.dkz_otf = 1 / (nz_otf * dz_psf);
+  s.od.nx_otf = nx_otf;
+  s.od.ny_otf = ny_otf;
+  s.od.nz_otf = nz_otf;
+  int rc;
+  if ((rc = ensure_stream(s))) return rc;
+  const size_t notf = (size_t)nx_otf * ny_otf * nz_otf;
+  if ((rc = s.raw_otf.ensure(notf))) return rc;
+  CDX_CHECK(cudaMemcpy(s.raw_otf.p, otf.data.data(), notf * sizeof(float2), cudaMemcpyHostToDevice));
+  // deskew geometry (RL-Biggs-Andrews.cpp:592-607)
+  s.deskewFactor = 0.;
+  s.deskewedXdim = s.output_nx;
+  if (fabs(deskewAngle) > 0.0) {
+    if (deskewAngle < 0) deskewAngle += 180.;
+    s.deskewFactor = cos(deskewAngle * M_PI / 180.) * dz / dr;
+    if (outputWidth == 0)
+      s.deskewedXdim += floor(s.output_nz * dz * fabs(cos(deskewAngle * M_PI / 180.)) / dr);
+    else
+      s.deskewedXdim = outputWidth;
+    s.deskewedXdim = find_optimal_dimension(s.deskewedXdim);
+    dz *= fabs(sin(deskewAngle * M_PI / 180.));
+  }
+  // rotation matrix (RL-Biggs-Andrews.cpp:609-619); the float overloads of
+  // cos/sin are the ones the reference's C++ resolves to
+  s.has_rot = false;
+  if (fabs(rotationAngle) > 0.0) {
+    s.has_rot = true;
+    rotationAngle *= M_PI / 180;
+    const float stretch = dr / dz;
+    s.rot[0] = cosf(rotationAngle) * stretch;
+    s.rot[1] = sinf(rotationAngle) * stretch;
+    s.rot[2] = -sinf(rotationAngle);
+    s.rot[3] = cosf(rotationAngle);
+  }
+  s.dr = dr;
+  s.dz = dz;
+  if (s.output_nx < 2 || s.output_ny < 2 || s.output_nz < 2 || s.deskewedXdim < 2) {
+    set_error("RL_interface_init", "no FFT-friendly size below the input size");
+    return cudaErrorInvalidValue;
+  }
+  // decon grid: deskewed width unless the decon runs on the skewed stack
+  const int gx = (bSkewedDecon && fabs(deskewAngle) > 0.0) ? (int)s.output_nx : (int)s.deskewedXdim;
+  if ((rc = ensure_plan(s, gx, s.output_ny, s.output_nz))) return rc;
+  s.inited = true;
+  return 0;
+}
+
+}  // namespace cdx
+
+using namespace cdx;
+
+extern "C" {
+
+int RL_interface_init(int nx, int ny, int nz, float dr, float dz, float dr_psf, float dz_psf,
+                      float deskewAngle, float rotationAngle, int outputWidth, bool bSkewedDecon,
+                      char* OTF_file_name) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return init_session(g_s, nx, ny, nz, dr, dz, dr_psf, dz_psf, deskewAngle, rotationAngle,
+                      outputWidth, bSkewedDecon, OTF_file_name) == 0
+             ? 1
+             : 0;
+}
+
+static int rl_common(const unsigned short* d_raw, const RLArgs& a, float* d_result,
+                     float* d_deskewed, float* h_result, float* h_deskewed) {
+  Session& s = g_s;
+  if (!s.inited) {
+    set_error("RL_interface", "RL_interface_init has not succeeded");
+    return cudaErrorInvalidValue;
+  }
+  const float* out = nullptr;
+  int dims[3];
+  int rc;
+  const size_t nd = (size_t)s.deskewedXdim * s.output_ny * s.output_nz;
+  float* desk_dev = d_deskewed;
+  if (h_deskewed && a.bSaveDeskewedRaw && fabs(s.deskewFactor) > 0.0) {
+    if ((rc = s.desk_stage.ensure(nd))) return rc;
+    desk_dev = s.desk_stage.p;
+  }
+  if ((rc = rl_pipeline(s, d_raw, a, desk_dev, &out, dims))) return rc;
+  size_t nout = (size_t)dims[0] * dims[1] * dims[2];
+  if (s.has_rot) {
+    // never write more than the get_output_n* sizes the caller allocated
+    const size_t cap = (size_t)reported_nx(s) * s.output_ny * reported_nz(s);
+    if (nout > cap) nout = cap;
+  }
+  if (h_result) {
+    CDX_CHECK(cudaMemcpyAsync(h_result, out, nout * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
+    if (h_deskewed && a.bSaveDeskewedRaw && fabs(s.deskewFactor) > 0.0 && desk_dev == s.desk_stage.p &&
+        !(a.bSkewedDecon && a.nIters > 0))
+      CDX_CHECK(cudaMemcpyAsync(h_deskewed, desk_dev, nd * sizeof(float), cudaMemcpyDeviceToHost,
+                                s.stream));
+    CDX_CHECK(cudaStreamSynchronize(s.stream));
+  } else if (d_result && out != d_result) {
+    CDX_CHECK(cudaMemcpyAsync(d_result, out, nout * sizeof(float), cudaMemcpyDeviceToDevice,
+                              s.stream));
+  }
+  return 0;
+}
+
+int RL_interface(const unsigned short* const raw_data, int nx, int ny, int nz, float* result,
+                 float* raw_deskewed_result, float background, bool bDoRescale,
+                 bool bSaveDeskewedRaw, int nIters, int extraShift, int napodize, int nZblend,
+                 float padVal, bool bDupRevStack, bool bSkewedDecon) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  s.launches = 0;
+  if (!raw_data || !result || nx < 1 || ny < 1 || nz < 1) {
+    set_error("RL_interface", "null pointer or empty stack");
+    return 0;
+  }
+  if (ensure_stream(s)) return 0;
+  const size_t nin = (size_t)nx * ny * nz;
+  if (s.u16in.ensure(nin)) return 0;
+  if (cudaMemcpyAsync(s.u16in.p, raw_data, nin * sizeof(unsigned short), cudaMemcpyHostToDevice,
+                      s.stream) != cudaSuccess) {
+    set_error("RL_interface", "host to device copy failed");
+    return 0;
+  }
+  RLArgs a{nx, ny, nz, background, bDoRescale, bSaveDeskewedRaw, nIters, extraShift,
+           napodize, nZblend, padVal, bDupRevStack, bSkewedDecon};
+  return rl_common(s.u16in.p, a, nullptr, nullptr, result, raw_deskewed_result) == 0 ? 1 : 0;
+}
+
+int cdx_RL_device(const unsigned short* raw_data, int nx, int ny, int nz, float* result,
+                  float* raw_deskewed_result, float background, bool bDoRescale,
+                  bool bSaveDeskewedRaw, int nIters, int extraShift, int napodize, int nZblend,
+                  float padVal, bool bDupRevStack, bool bSkewedDecon, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  s.launches = 0;
+  if (!raw_data || !result) {
+    set_error("cdx_RL_device", "null pointer");
+    return 0;
+  }
+  if (ensure_stream(s)) return 0;
+  // run on the caller's stream
+  cudaStream_t own = s.stream;
+  s.stream = (cudaStream_t)stream;
+  RLArgs a{nx, ny, nz, background, bDoRescale, bSaveDeskewedRaw, nIters, extraShift,
+           napodize, nZblend, padVal, bDupRevStack, bSkewedDecon};
+  int rc = rl_common(raw_data, a, result, raw_deskewed_result, nullptr, nullptr);
+  s.stream = own;
+  return rc == 0 ? 1 : 0;
+}
+
+long long cdx_last_launch_count(void) { return g_s.launches; }
+
+int cdx_profile_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  prof_collect();
+  Profiler& P = g_prof;
+  P.on = on != 0;
+  for (int p = 0; p < kPasses; ++p) {
+    P.pass_ms[p] = 0;
+    P.pass_n[p] = 0;
+  }
+  P.iter_ms = 0;
+  P.iter_n = 0;
+  return 1;
+}
+
+int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, double* iter_ms,
+                     long long* iter_count) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  prof_collect();
+  Profiler& P = g_prof;
+  for (int p = 0; p < kPasses && p < max_passes; ++p) {
+    if (pass_ms) pass_ms[p] = P.pass_ms[p];
+    if (pass_count) pass_count[p] = P.pass_n[p];
+  }
+  if (iter_ms) *iter_ms = P.iter_ms;
+  if (iter_count) *iter_count = P.iter_n;
+  return kPasses;
+}
+
+const char* cdx_profile_pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : ""; }
+
+void RL_cleanup(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  s.intensity_overall0 = 0.;
+  s.bFirstTime = true;
+  s.plan.release();
+  s.raw_otf.release();
+  s.has_rot = false;
+  s.inited = false;
+  // release the large work buffers too (the reference frees them per call)
+  s.Xa.release();
+  s.Xb.release();
+  s.G.release();
+  s.raw.release();
+  s.S.release();
+  s.pre.release();
+  s.u16in.release();
+  s.rotbuf.release();
+  s.desk_stage.release();
+  s.res_stage.release();
+  s.conv_tmp.release();
+}
+
+void cuda_reset(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  release_all(g_s);
+  g_s.inited = false;
+  g_s.intensity_overall0 = 0.;
+  g_s.bFirstTime = true;
+  cudaDeviceReset();
+}
+
+int cdx_decon_grid(int* nx, int* ny, int* nz) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_s.inited || !g_s.plan.valid) {
+    set_error("cdx_decon_grid", "RL_interface_init has not succeeded");
+    return 0;
+  }
+  if (nx) *nx = g_s.plan.g.nx;
+  if (ny) *ny = g_s.plan.g.ny;
+  if (nz) *nz = g_s.plan.g.nz;
+  return 1;
+}
+
+unsigned get_output_nx(void) { return reported_nx(g_s); }
+unsigned get_output_ny(void) { return g_s.output_ny; }
+unsigned get_output_nz(void) { return reported_nz(g_s); }
+
+const char* get_version(void) { return "0.7.0-gb300"; }
+
+const char* cdx_last_error(void) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_err_shared.c_str();
+}
+
+int Deskew_interface(const float* const raw_data, int nx, int ny, int nz, float dz, float dr,
+                     float deskewAngle, float* const result, int outputWidth, int extraShift,
+                     float padVal) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!raw_data || !result || nx < 1 || ny < 1 || nz < 1) {
+    set_error("Deskew_interface", "null pointer or empty stack");
+    return 0;
+  }
+  // RL-Biggs-Andrews.cpp:731-744 (output_nz is the RL_interface_init global)
+  double deskewFactor = 0.;
+  unsigned deskewedXdim = nx;
+  if (fabs(deskewAngle) > 0.0) {
+    if (deskewAngle < 0) deskewAngle += 180.;
+    deskewFactor = cos(deskewAngle * M_PI / 180.) * dz / dr;
+    if (outputWidth == 0)
+      deskewedXdim += floor(s.output_nz * dz * fabs(cos(deskewAngle * M_PI / 180.)) / dr) / 4.;
+    else
+      deskewedXdim = outputWidth;
+  }
+  if (ensure_stream(s)) return 0;
+  DevBuf<float> din, dout;
+  const size_t nin = (size_t)nx * ny * nz, nout = (size_t)deskewedXdim * ny * nz;
+  if (din.ensure(nin) || dout.ensure(nout)) return 0;
+  int ok = 1;
+  if (cudaMemcpyAsync(din.p, raw_data, nin * sizeof(float), cudaMemcpyHostToDevice, s.stream) ||
+      launch_deskew(din.p, nx, ny, nz, deskewFactor, dout.p, deskewedXdim, extraShift, padVal,
+                    s.stream) ||
+      cudaMemcpyAsync(result, dout.p, nout * sizeof(float), cudaMemcpyDeviceToHost, s.stream) ||
+      cudaStreamSynchronize(s.stream))
+    ok = 0;
+  din.release();
+  dout.release();
+  return ok;
+}
+
+int cdx_deskew_device(const float* in, int nx, int ny, int nz, double deskewFactor, float* out,
+                      int nxOut, int extraShift, float padVal, void* stream) {
+  return launch_deskew(in, nx, ny, nz, deskewFactor, out, nxOut, extraShift, padVal,
+                       (cudaStream_t)stream) == 0
+             ? 1
+             : 0;
+}
+
+int cdx_rotate_device(const float* in, int nx, int ny, int nz, const float* rot, float* out,
+                      int nx_out, int nz_out, void* stream) {
+  return launch_rotate(in, nx, ny, nz, rot, out, nx_out, nz_out, (cudaStream_t)stream) == 0 ? 1 : 0;
+}
+
+int cdx_camcor_device(const unsigned short* raw, int nx, int ny, int nz, const float* camparam,
+                      unsigned short* out, void* stream) {
+  return launch_camcor(raw, nx, ny, nz, camparam, out, (cudaStream_t)stream) == 0 ? 1 : 0;
+}
+
+int camcor_interface_init(int nx, int ny, int nz, const float* const camparam) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!camparam || nx < 1 || ny < 1 || nz < 1) {
+    set_error("camcor_interface_init", "null pointer or empty size");
+    return 0;
+  }
+  if (ensure_stream(s)) return 0;
+  const size_t np = (size_t)nx * ny * 3;
+  if (s.cc_param.ensure(np)) return 0;
+  if (cudaMemcpy(s.cc_param.p, camparam, np * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+    set_error("camcor_interface_init", "copy failed");
+    return 0;
+  }
+  s.cc_nx = nx;
+  s.cc_ny = ny;
+  s.cc_nz = nz;
+  return 1;
+}
+
+int camcor_interface(const unsigned short* const raw_data, int nx, int ny, int nz,
+                     unsigned short* const result) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!s.cc_param.p) {
+    set_error("camcor_interface", "camcor_interface_init has not succeeded");
+    return 0;
+  }
+  if (nx != s.cc_nx || ny != s.cc_ny || nz != s.cc_nz || !raw_data || !result) {
+    set_error("camcor_interface", "sizes differ from camcor_interface_init");
+    return 0;
+  }
+  const size_t n = (size_t)nx * ny * nz;
+  if (s.cc_in.ensure(n) || s.cc_out.ensure(n)) return 0;
+  if (cudaMemcpyAsync(s.cc_in.p, raw_data, n * 2, cudaMemcpyHostToDevice, s.stream) ||
+      launch_camcor(s.cc_in.p, nx, ny, nz, s.cc_param.p, s.cc_out.p, s.stream) ||
+      cudaMemcpyAsync(result, s.cc_out.p, n * 2, cudaMemcpyDeviceToHost, s.stream) ||
+      cudaStreamSynchronize(s.stream)) {
+    set_error("camcor_interface", "CUDA failure");
+    return 0;
+  }
+  return 1;
+}
+
+int Affine_interface(const float* const raw_data, int nx, int ny, int nz, float* const result,
+                     const float* affMat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!raw_data || !result || !affMat || nx < 1 || ny < 1 || nz < 1) {
+    set_error("Affine_interface", "null pointer or empty stack");
+    return 0;
+  }
+  if (ensure_stream(g_s)) return 0;
+  return affine_host(raw_data, nx, ny, nz, affMat, false, 1.f, 1.f, 1.f, result, g_s.stream) == 0;
+}
+
+int Affine_interface_RA(const float* const raw_data, int nx, int ny, int nz, float dx, float dy,
+                        float dz, float* const result, const float* affMat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!raw_data || !result || !affMat || nx < 1 || ny < 1 || nz < 1) {
+    set_error("Affine_interface_RA", "null pointer or empty stack");
+    return 0;
+  }
+  if (ensure_stream(g_s)) return 0;
+  return affine_host(raw_data, nx, ny, nz, affMat, true, dx, dy, dz, result, g_s.stream) == 0;
+}
+
+int cdx_fft_length_supported(int n) { return fft_len_supported(n) ? 1 : 0; }
+
+int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
+                   size_t capacity) {
+  HostImage img;
+  std::string err;
+  if (!load_image_file(path, img, err)) {
+    set_error("cdx_load_image", err.c_str());
+    return 0;
+  }
+  if (width) *width = img.w;
+  if (height) *height = img.h;
+  if (depth) *depth = img.d;
+  if (out) {
+    if (capacity < img.data.size()) {
+      set_error("cdx_load_image", "output buffer too small");
+      return 0;
+    }
+    memcpy(out, img.data.data(), img.data.size() * sizeof(float));
+  }
+  return 1;
+}
+
+int cdx_rfft3d_device(const float* in, void* out_complex, int nx, int ny, int nz, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t st = (cudaStream_t)stream;
+  Geom g = make_geom(nx, ny, nz);
+  FftLen fx, fy, fz;
+  DevBuf<float2> S;
+  OtfDev none{};
+  int ok = !(fft_len_init(fx, nx) || fft_len_init(fy, ny) || fft_len_init(fz, nz) ||
+             S.ensure((size_t)g.spec_elems()) ||
+             launch_x_fwd(g, fx, in, nullptr, nullptr, 0, S.p, st) ||
+             launch_y_pass(g, fy, S.p, false, st) || launch_z_pass(g, fz, S.p, none, false, st, true) ||
+             launch_spec_to_std(g, S.p, (float2*)out_complex, st) || cudaStreamSynchronize(st));
+  fft_len_free(fx);
+  fft_len_free(fy);
+  fft_len_free(fz);
+  S.release();
+  return ok;
+}
+
+int cdx_conv3d_device(const float* in, float* out, int nx, int ny, int nz, int conj, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!s.raw_otf.p) {
+    set_error("cdx_conv3d_device", "RL_interface_init has not succeeded");
+    return 0;
+  }
+  if (ensure_stream(s) || ensure_plan(s, nx, ny, nz)) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const GridPlan& p = s.plan;
+  DevBuf<float2> S;
+  int ok = !(S.ensure((size_t)p.g.spec_elems()) ||
+             launch_x_fwd(p.g, p.fx, in, nullptr, nullptr, 0, S.p, st) ||
+             launch_y_pass(p.g, p.fy, S.p, false, st) ||
+             launch_z_pass(p.g, p.fz, S.p, p.otf, conj != 0, st) ||
+             launch_y_pass(p.g, p.fy, S.p, true, st) || launch_x_inv_plain(p.g, p.fx, S.p, out, st) ||
+             cudaStreamSynchronize(st));
+  S.release();
+  return ok;
+}
+
+}  // extern "C"

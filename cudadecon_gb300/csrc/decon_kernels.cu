@@ -1,0 +1,619 @@
+// The Richardson-Lucy / Biggs-Andrews hot loop as fused FFT passes.
+//
+// One iteration of the reference (src/RL-Biggs-Andrews.cpp:282-367) is
+//   Y   = k>1 ? max(X + lambda*(X - X_{k-1}), 0) : X        (RLgpuImpl.cu:658-666)
+//   CC  = C2R(R2C(Y/N) * OTF)                                (RLgpuImpl.cu:156-225, 331-339)
+//   CC  = clamp(raw / (|CC|>0 ? CC : eps) + eps, -10, 10)    (RLgpuImpl.cu:416-434)
+//   CC  = C2R(R2C(CC/N) * conj(OTF))                         (RLgpuImpl.cu:341-350)
+//   X   = max(CC*Y, 0); G = X - Y                            (RLgpuImpl.cu:462-470, 501-508)
+//   lambda_next = (G.G_old)/(G_old.G_old + eps), in [0,1]    (RLgpuImpl.cu:510-633)
+// Here it runs as nine kernels: x_fwd (with the prediction prologue), y, z
+// (fwd * OTF * inv), y, x_inv+ratio+x_fwd, y, z (conj), y, x_inv+update (with
+// the FP64 dot products and an on-device lambda).  The 1/N normalisation is
+// folded into the OTF table.  No intermediate real volume is written between
+// the two convolutions.
+#include "kernels.h"
+
+#include <math.h>
+#include <vector>
+
+namespace cdx {
+
+Geom make_geom(int nx, int ny, int nz) {
+  Geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.nxh = nx / 2 + 1;
+  g.nyp = ny + (ny & 1);
+  g.plane = (long long)nz * g.nyp;
+  return g;
+}
+
+// ---------------------------------------------------------------- FFT plans
+static bool factorize(int L, std::vector<int>& rad) {
+  rad.clear();
+  int n = L;
+  int p2 = 0;
+  while (n % 2 == 0) { n /= 2; ++p2; }
+  while (p2 >= 4) { rad.push_back(16); p2 -= 4; }
+  if (p2 == 3) rad.push_back(8);
+  else if (p2 == 2) rad.push_back(4);
+  else if (p2 == 1) rad.push_back(2);
+  while (n % 9 == 0) { rad.push_back(9); n /= 9; }
+  while (n % 3 == 0) { rad.push_back(3); n /= 3; }
+  while (n % 7 == 0) { rad.push_back(7); n /= 7; }
+  while (n % 5 == 0) { rad.push_back(5); n /= 5; }
+  if (n != 1) return false;
+  if ((int)rad.size() > kMaxStages) return false;
+  if (rad.empty()) rad.push_back(1);  // L == 1: identity
+  return true;
+}
+
+bool fft_len_supported(int L) {
+  std::vector<int> r;
+  return L >= 1 && L <= kMaxFftLen && factorize(L, r);
+}
+
+int fft_len_init(FftLen& f, int L) {
+  std::vector<int> rad;
+  if (L < 1 || L > kMaxFftLen || !factorize(L, rad)) {
+    set_error("fft_len_init", "length is not a product of 2, 3, 5 and 7");
+    return cudaErrorInvalidValue;
+  }
+  f.dev.L = L;
+  f.dev.nst = (rad.size() == 1 && rad[0] == 1) ? 0 : (int)rad.size();
+  for (int i = 0; i < kMaxStages; ++i) f.dev.radix[i] = i < (int)rad.size() ? rad[i] : 1;
+  std::vector<float2> tw(L);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int m = 0; m < L; ++m) {
+    const double a = -two_pi * (double)m / (double)L;
+    tw[m] = make_float2((float)cos(a), (float)sin(a));
+  }
+  CDX_CHECK(cudaMalloc(&f.d_tw, sizeof(float2) * L));
+  CDX_CHECK(cudaMemcpy(f.d_tw, tw.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+  f.dev.tw = f.d_tw;
+  return 0;
+}
+
+void fft_len_free(FftLen& f) {
+  if (f.d_tw) cudaFree(f.d_tw);
+  f.d_tw = nullptr;
+  f.dev.tw = nullptr;
+}
+
+// ---------------------------------------------------------------- helpers
+// Prediction of the reference's updatePrediction_kernel (RLgpuImpl.cu:658-666):
+// Y = X + lambda*(X - X_{k-1}) with lambda as float, then clamped at 0.
+__device__ __forceinline__ float predict_y(float x, float xm1, float lam) {
+  float y = __fmaf_rn(lam, __fsub_rn(x, xm1), x);
+  return y > 0.f ? y : 0.f;
+}
+
+// Split the FFT Z of packed rows (a + i b) into the half spectra of a and b.
+__device__ __forceinline__ float4 split_pair(float2 zk, float2 zm) {
+  // A = (Z[k] + conj(Z[n-k]))/2, B = (Z[k] - conj(Z[n-k]))/(2i)
+  return make_float4(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y), 0.5f * (zk.y + zm.y),
+                     0.5f * (zm.x - zk.x));
+}
+
+// Row pairs per x tile: up to 8 (16 rows -> 128-byte spectrum runs), fewer
+// for long rows so that the tile fits kMaxThreads * kEpt elements.
+static int x_pairs(int nx) {
+  int p = (kMaxThreads * kEpt) / nx;
+  if (p > 8) p = 8;
+  if (p < 1) p = 1;
+  return p;
+}
+
+int x_pass_blocks(const Geom& g) { return ceil_div(g.ny, 2 * x_pairs(g.nx)) * g.nz; }
+
+static int threads_for(long long elems) {
+  long long t = (elems + kEpt - 1) / kEpt;
+  t = ((t + 31) / 32) * 32;
+  if (t < 64) t = 64;
+  if (t > kMaxThreads) t = kMaxThreads;
+  return (int)t;
+}
+
+// Store the packed-row FFT held in sm (P vectors of length nx) into S.
+__device__ __forceinline__ void store_half_spectra(const Geom& g, const float2* sm, int P, int z,
+                                                   int y0, float2* S) {
+  const int nx = g.nx;
+  for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
+    const int p = idx % P;
+    const int k = idx / P;
+    const int ya = y0 + 2 * p;
+    if (ya >= g.ny) continue;
+    const float2 zk = sm[p * nx + k];
+    const float2 zm = sm[p * nx + (k == 0 ? 0 : nx - k)];
+    float4 v = split_pair(zk, zm);
+    *reinterpret_cast<float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya) = v;
+  }
+}
+
+// Load the two half spectra of rows (ya, ya+1) and rebuild the packed
+// full-length spectrum Z = A + iB in sm.  The imaginary parts of the DC and
+// (even nx) Nyquist bins are dropped, as a C2R transform does.
+__device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2* S, float2* sm,
+                                                    int P, int z, int y0) {
+  const int nx = g.nx;
+  for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
+    const int p = idx % P;
+    const int k = idx / P;
+    const int ya = y0 + 2 * p;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ya < g.ny)
+      v = *reinterpret_cast<const float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya);
+    if (k == 0 || 2 * k == nx) {
+      v.y = 0.f;
+      v.w = 0.f;
+    }
+    // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
+    sm[p * nx + k] = make_float2(v.x - v.w, v.y + v.z);
+    if (k > 0 && 2 * k != nx) sm[p * nx + nx - k] = make_float2(v.x + v.w, v.z - v.y);
+  }
+}
+
+// ---------------------------------------------------------------- x forward
+__global__ void __launch_bounds__(kMaxThreads, 1) k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X,
+                        const float* __restrict__ Xm1, const float* __restrict__ lamp, int predict,
+                        float2* __restrict__ S, int P) {
+  extern __shared__ float2 sm[];
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * P;
+  const int nx = g.nx;
+  const float lam = predict ? __ldg(lamp) : 0.f;
+  const long long zoff = (long long)z * g.ny * nx;
+  for (int idx = threadIdx.x; idx < P * nx; idx += blockDim.x) {
+    const int p = idx / nx;
+    const int n = idx - p * nx;
+    const int ya = y0 + 2 * p;
+    float a = 0.f, b = 0.f;
+    if (ya < g.ny) {
+      const long long o = zoff + (long long)ya * nx + n;
+      a = __ldg(X + o);
+      if (predict) a = predict_y(a, __ldg(Xm1 + o), lam);
+      if (ya + 1 < g.ny) {
+        b = __ldg(X + o + nx);
+        if (predict) b = predict_y(b, __ldg(Xm1 + o + nx), lam);
+      }
+    }
+    sm[idx] = make_float2(a, b);
+  }
+  __syncthreads();
+  fft_tile<false>(sm, fx, P, 1, nx, false);
+  store_half_spectra(g, sm, P, z, y0, S);
+}
+
+int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* Xm1,
+                 const float* lam, int predict, float2* S, cudaStream_t st) {
+  const int P = x_pairs(g.nx);
+  dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
+  int T = threads_for((long long)P * g.nx);
+  size_t smem = sizeof(float2) * P * g.nx;
+  k_x_fwd<<<grid, T, smem, st>>>(g, fx.dev, X, Xm1, lam, predict, S, P);
+  CDX_LAUNCH_CHECK("k_x_fwd");
+  return 0;
+}
+
+// ---------------------------------------------------------------- y pass
+template <bool INV>
+__global__ void __launch_bounds__(kMaxThreads, 1) k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
+  extern __shared__ float2 sm[];
+  const int ny = g.ny;
+  const long long nrows = (long long)g.nxh * g.nz;
+  const long long r0 = (long long)blockIdx.x * V;
+  // rows r0..r0+V-1, row r at S + r*nyp (kx = r / nz, z = r % nz; plane = nz*nyp)
+  for (int idx = threadIdx.x; idx < V * ny; idx += blockDim.x) {
+    const int v = idx / ny;
+    const int e = idx - v * ny;
+    const long long r = r0 + v;
+    sm[idx] = r < nrows ? S[r * g.nyp + e] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_tile<INV>(sm, fy, V, 1, ny, false);
+  for (int idx = threadIdx.x; idx < V * ny; idx += blockDim.x) {
+    const int v = idx / ny;
+    const int e = idx - v * ny;
+    const long long r = r0 + v;
+    if (r < nrows) S[r * g.nyp + e] = sm[idx];
+  }
+}
+
+int launch_y_pass(const Geom& g, const FftLen& fy, float2* S, bool inverse, cudaStream_t st) {
+  int V = 2048 / g.ny;
+  if (V < 1) V = 1;
+  const long long nrows = (long long)g.nxh * g.nz;
+  int T = threads_for((long long)V * g.ny);
+  size_t smem = sizeof(float2) * V * g.ny;
+  dim3 grid((unsigned)((nrows + V - 1) / V));
+  if (inverse)
+    k_y_pass<true><<<grid, T, smem, st>>>(g, fy.dev, S, V);
+  else
+    k_y_pass<false><<<grid, T, smem, st>>>(g, fy.dev, S, V);
+  CDX_LAUNCH_CHECK("k_y_pass");
+  return 0;
+}
+
+// ---------------------------------------------------------------- z pass
+// Columns (consecutive y) per z tile: 16 (128-byte runs) while the tile fits
+// kMaxThreads * kEpt elements, fewer for long z.
+static int z_cols(int nz) {
+  int w = (kMaxThreads * kEpt) / nz;
+  if (w > 16) w = 16;
+  if (w < 1) w = 1;
+  return w;
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1) k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj,
+                         int fwd_only, int W) {
+  extern __shared__ float2 sm[];
+  const int kx = blockIdx.y;
+  const int y0 = blockIdx.x * W;
+  const int nz = g.nz;
+  float2* base = S + (long long)kx * g.plane;
+  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+    const int w = idx % W;
+    const int z = idx / W;
+    const int y = y0 + w;
+    sm[idx] = y < g.ny ? base[(long long)z * g.nyp + y] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_tile<false>(sm, fz, W, W, 1, true);
+  if (fwd_only) {
+    for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+      const int w = idx % W;
+      const int z = idx / W;
+      const int y = y0 + w;
+      if (y < g.ny) base[(long long)z * g.nyp + y] = sm[idx];
+    }
+    return;
+  }
+  // multiply by the OTF, interpolated on the fly (RA) or read (3D)
+  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+    const int w = idx % W;
+    const int z = idx / W;
+    const int y = y0 + w;
+    if (y >= g.ny) continue;
+    float2 o;
+    if (otf.mode == 1) {
+      o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
+    } else {
+      // reference dev_otfinterpolate RA branch (RLgpuImpl.cu:238-273):
+      // kr = sqrt(kx^2 + ky^2) in OTF radial samples, zero outside nr-1
+      const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+      const float fx = (float)kx * otf.kxscale;
+      const float fy = (float)ky * otf.kyscale;
+      const float kr = sqrtf(fx * fx + fy * fy);
+      if (kr < (float)(otf.nr - 1)) {
+        const int ir = (int)floorf(kr);
+        const float ar = kr - (float)ir;
+        const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
+        const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
+        o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+      } else {
+        o = make_float2(0.f, 0.f);
+      }
+    }
+    sm[idx] = conj ? cmulconj(sm[idx], o) : cmul(sm[idx], o);
+  }
+  __syncthreads();
+  fft_tile<true>(sm, fz, W, W, 1, true);
+  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+    const int w = idx % W;
+    const int z = idx / W;
+    const int y = y0 + w;
+    if (y < g.ny) base[(long long)z * g.nyp + y] = sm[idx];
+  }
+}
+
+int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf, bool conj,
+                  cudaStream_t st, bool fwd_only) {
+  const int W = z_cols(g.nz);
+  dim3 grid(ceil_div(g.ny, W), g.nxh);
+  int T = threads_for((long long)W * g.nz);
+  size_t smem = sizeof(float2) * W * g.nz;
+  k_z_pass<<<grid, T, smem, st>>>(g, fz.dev, S, otf, conj ? 1 : 0, fwd_only ? 1 : 0, W);
+  CDX_LAUNCH_CHECK("k_z_pass");
+  return 0;
+}
+
+// ---------------------------------------------------------------- x inverse
+__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S,
+                                  const float* __restrict__ raw, float eps, int P) {
+  extern __shared__ float2 sm[];
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * P;
+  const int nx = g.nx;
+  load_packed_spectra(g, S, sm, P, z, y0);
+  __syncthreads();
+  fft_tile<true>(sm, fx, P, 1, nx, false);
+  // RL ratio of the reference's LRcore_kernel (RLgpuImpl.cu:416-434)
+  const long long zoff = (long long)z * g.ny * nx;
+  for (int idx = threadIdx.x; idx < P * nx; idx += blockDim.x) {
+    const int p = idx / nx;
+    const int n = idx - p * nx;
+    const int ya = y0 + 2 * p;
+    float2 c = sm[idx];
+    float2 r = make_float2(0.f, 0.f);
+    if (ya < g.ny) {
+      const long long o = zoff + (long long)ya * nx + n;
+      float v = fabsf(c.x) > 0.f ? c.x : eps;
+      v = __fadd_rn(__fdiv_rn(__ldg(raw + o), v), eps);
+      v = v > 10.f ? 10.f : v;
+      v = v < -10.f ? -10.f : v;
+      r.x = v;
+      if (ya + 1 < g.ny) {
+        float u = fabsf(c.y) > 0.f ? c.y : eps;
+        u = __fadd_rn(__fdiv_rn(__ldg(raw + o + nx), u), eps);
+        u = u > 10.f ? 10.f : u;
+        u = u < -10.f ? -10.f : u;
+        r.y = u;
+      }
+    }
+    sm[idx] = r;
+  }
+  __syncthreads();
+  fft_tile<false>(sm, fx, P, 1, nx, false);
+  store_half_spectra(g, sm, P, z, y0, S);
+}
+
+int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const float* raw,
+                           float eps, cudaStream_t st) {
+  const int P = x_pairs(g.nx);
+  dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
+  int T = threads_for((long long)P * g.nx);
+  size_t smem = sizeof(float2) * P * g.nx;
+  k_x_inv_ratio_fwd<<<grid, T, smem, st>>>(g, fx.dev, S, raw, eps, P);
+  CDX_LAUNCH_CHECK("k_x_inv_ratio_fwd");
+  return 0;
+}
+
+// Block-wide sum of two doubles; result valid in thread 0.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    red[warp] = a;
+    red[32 + warp] = b;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < nw ? red[lane] : 0.0;
+    b = lane < nw ? red[32 + lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S,
+                               const float* __restrict__ X, const float* Xm1,
+                               const float* __restrict__ lamp, int predict, float* Xout,
+                               float* __restrict__ G, int dots, double* partials,
+                               unsigned* counter, float* lam_next, float eps, int P) {
+  extern __shared__ float2 sm[];
+  __shared__ double red[64];
+  __shared__ bool last;
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * P;
+  const int nx = g.nx;
+  const float lam = predict ? __ldg(lamp) : 0.f;
+  load_packed_spectra(g, S, sm, P, z, y0);
+  __syncthreads();
+  fft_tile<true>(sm, fx, P, 1, nx, false);
+  const long long zoff = (long long)z * g.ny * nx;
+  double s1 = 0.0, s2 = 0.0;
+  for (int idx = threadIdx.x; idx < 2 * P * nx; idx += blockDim.x) {
+    const int rr = idx / nx;  // row within the tile
+    const int n = idx - rr * nx;
+    const int y = y0 + rr;
+    if (y >= g.ny) continue;
+    const float2 c2 = sm[(rr >> 1) * nx + n];
+    const float cc = (rr & 1) ? c2.y : c2.x;
+    const long long o = zoff + (long long)y * nx + n;
+    const float x = X[o];
+    const float yv = predict ? predict_y(x, Xm1[o], lam) : x;
+    float xn = __fmul_rn(cc, yv);
+    xn = xn > 0.f ? xn : 0.f;
+    const float gn = __fsub_rn(xn, yv);
+    if (dots) {
+      const float go = G[o];
+      s1 += (double)__fmul_rn(gn, go);
+      s2 += (double)__fmul_rn(go, go);
+    }
+    Xout[o] = xn;
+    G[o] = gn;
+  }
+  if (!dots) return;
+  block_sum2(s1, s2, red);
+  const int nblk = gridDim.x * gridDim.y;
+  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  if (threadIdx.x == 0) {
+    partials[bid] = s1;
+    partials[nblk + bid] = s2;
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == (unsigned)nblk - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  // Last block: reduce all partials in a fixed order (deterministic).
+  __threadfence();
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    a += __ldcg(partials + i);
+    b += __ldcg(partials + nblk + i);
+  }
+  block_sum2(a, b, red);
+  if (threadIdx.x == 0) {
+    // calcAccelFactor (RLgpuImpl.cu:565) then the clamp of RL-Biggs-Andrews.cpp:298
+    double l = a / (b + (double)eps);
+    l = (1.0 < l) ? 1.0 : l;
+    l = (l < 0.0) ? 0.0 : l;
+    *lam_next = (float)l;
+    *counter = 0u;
+  }
+}
+
+int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* X,
+                        const float* Xm1, const float* lam, int predict, float* Xout, float* G,
+                        int dots, RLWork& w, float* lam_next, float eps, cudaStream_t st) {
+  const int P = x_pairs(g.nx);
+  dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
+  const int nblk = grid.x * grid.y;
+  if (dots && nblk > w.max_blocks) {
+    set_error("launch_x_inv_update", "partials buffer too small");
+    return cudaErrorInvalidValue;
+  }
+  int T = threads_for((long long)P * g.nx);
+  size_t smem = sizeof(float2) * P * g.nx;
+  k_x_inv_update<<<grid, T, smem, st>>>(g, fx.dev, S, X, Xm1, lam, predict, Xout, G, dots,
+                                        w.partials, w.counter, lam_next, eps, P);
+  CDX_LAUNCH_CHECK("k_x_inv_update");
+  return 0;
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S,
+                              float* __restrict__ out, int P) {
+  extern __shared__ float2 sm[];
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * P;
+  const int nx = g.nx;
+  load_packed_spectra(g, S, sm, P, z, y0);
+  __syncthreads();
+  fft_tile<true>(sm, fx, P, 1, nx, false);
+  const long long zoff = (long long)z * g.ny * nx;
+  for (int idx = threadIdx.x; idx < 2 * P * nx; idx += blockDim.x) {
+    const int rr = idx / nx;
+    const int n = idx - rr * nx;
+    const int y = y0 + rr;
+    if (y >= g.ny) continue;
+    const float2 c2 = sm[(rr >> 1) * nx + n];
+    out[zoff + (long long)y * nx + n] = (rr & 1) ? c2.y : c2.x;
+  }
+}
+
+int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* out,
+                       cudaStream_t st) {
+  const int P = x_pairs(g.nx);
+  dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
+  int T = threads_for((long long)P * g.nx);
+  size_t smem = sizeof(float2) * P * g.nx;
+  k_x_inv_plain<<<grid, T, smem, st>>>(g, fx.dev, S, out, P);
+  CDX_LAUNCH_CHECK("k_x_inv_plain");
+  return 0;
+}
+
+__global__ void k_spec_to_std(Geom g, const float2* __restrict__ S, float2* __restrict__ out) {
+  const long long n = (long long)g.nz * g.ny * g.nxh;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % g.nxh);
+    const long long r = i / g.nxh;
+    const int y = (int)(r % g.ny);
+    const int z = (int)(r / g.ny);
+    out[i] = S[(long long)kx * g.plane + (long long)z * g.nyp + y];
+  }
+}
+
+int launch_spec_to_std(const Geom& g, const float2* S, float2* out, cudaStream_t st) {
+  k_spec_to_std<<<1216, 256, 0, st>>>(g, S, out);
+  CDX_LAUNCH_CHECK("k_spec_to_std");
+  return 0;
+}
+
+// ---------------------------------------------------------------- OTF tables
+// Radially averaged OTF resampled along kz for every z frequency of the
+// volume: tz[ir][z] = otf[ir][iz]*(1-az) + otf[ir][iz+1 (wrapping)]*az, zero
+// where kzindex falls outside [0, nz_otf), times scale (= 1/N).
+// Follows dev_otfinterpolate's RA branch (RLgpuImpl.cu:233-273) with the kz
+// coordinate of makeOTFarray_kernel (RLgpuImpl.cu:357).
+__global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2* __restrict__ otf,
+                         float2* __restrict__ tz, float scale) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ir = blockIdx.y;
+  if (z >= nz) return;
+  const int kz = z > (nz >> 1) ? z - nz : z;
+  const float fz = (float)kz * kzscale;
+  const float kzindex = fz < 0.f ? fz + (float)nzotf : fz;
+  float2 v = make_float2(0.f, 0.f);
+  if (kzindex < (float)nzotf && kzindex >= 0.f) {
+    const int iz = (int)floorf(kzindex);
+    const float az = kzindex - (float)iz;
+    const int izp = (iz == nzotf - 1) ? 0 : iz + 1;
+    const float2 a = otf[(long long)ir * nzotf + iz];
+    const float2 b = otf[(long long)ir * nzotf + izp];
+    v = make_float2(a.x * (1.f - az) + b.x * az, a.y * (1.f - az) + b.y * az);
+  }
+  tz[(long long)ir * nz + z] = make_float2(v.x * scale, v.y * scale);
+}
+
+int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* tz,
+                  float scale, cudaStream_t st) {
+  dim3 grid(ceil_div(g.nz, 128), od.nx_otf);
+  k_otf_tz<<<grid, 128, 0, st>>>(g.nz, od.nx_otf, od.nz_otf, od.kzscale, raw_otf, tz, scale);
+  CDX_LAUNCH_CHECK("k_otf_tz");
+  return 0;
+}
+
+// Full 3D (non radially averaged) OTF: trilinear with y/z wrap, as the
+// non-RA branch of dev_otfinterpolate (RLgpuImpl.cu:274-319), laid out in the
+// spectrum order and scaled.
+__global__ void k_otf_full(Geom g, int nxotf, int nyotf, int nzotf, float kxs, float kys, float kzs,
+                           const float2* __restrict__ otf, float2* __restrict__ full, float scale) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  const int z = blockIdx.y;
+  const int kx = blockIdx.z;
+  if (y >= g.ny) return;
+  const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+  const int kz = z > (g.nz >> 1) ? z - g.nz : z;
+  const float kxindex = (float)kx * kxs;
+  const float fy = (float)ky * kys;
+  const float fz = (float)kz * kzs;
+  const float kyindex = fy < 0.f ? fy + (float)nyotf : fy;
+  const float kzindex = fz < 0.f ? fz + (float)nzotf : fz;
+  float2 v = make_float2(0.f, 0.f);
+  if (kxindex < (float)(nxotf - 1) && kyindex < (float)nyotf && kzindex < (float)nzotf &&
+      kyindex >= 0.f && kzindex >= 0.f) {
+    const int ix = (int)floorf(kxindex), iy = (int)floorf(kyindex), iz = (int)floorf(kzindex);
+    const int iy1 = (iy + 1) % nyotf, iz1 = (iz + 1) % nzotf;
+    const float ax = kxindex - ix, ay = kyindex - iy, az = kzindex - iz;
+    const long long nxy = (long long)nxotf * nyotf;
+    const float2 o000 = otf[iz * nxy + (long long)iy * nxotf + ix];
+    const float2 o001 = otf[iz * nxy + (long long)iy * nxotf + ix + 1];
+    const float2 o010 = otf[iz * nxy + (long long)iy1 * nxotf + ix];
+    const float2 o011 = otf[iz * nxy + (long long)iy1 * nxotf + ix + 1];
+    const float2 o100 = otf[iz1 * nxy + (long long)iy * nxotf + ix];
+    const float2 o101 = otf[iz1 * nxy + (long long)iy * nxotf + ix + 1];
+    const float2 o110 = otf[iz1 * nxy + (long long)iy1 * nxotf + ix];
+    const float2 o111 = otf[iz1 * nxy + (long long)iy1 * nxotf + ix + 1];
+    v.x = (1 - az) * (o000.x * (1 - ay) * (1 - ax) + o001.x * (1 - ay) * ax + o010.x * ay * (1 - ax) +
+                      o011.x * ay * ax) +
+          az * (o100.x * (1 - ay) * (1 - ax) + o101.x * (1 - ay) * ax + o110.x * ay * (1 - ax) +
+                o111.x * ay * ax);
+    v.y = (1 - az) * (o000.y * (1 - ay) * (1 - ax) + o001.y * (1 - ay) * ax + o010.y * ay * (1 - ax) +
+                      o011.y * ay * ax) +
+          az * (o100.y * (1 - ay) * (1 - ax) + o101.y * (1 - ay) * ax + o110.y * ay * (1 - ax) +
+                o111.y * ay * ax);
+  }
+  full[(long long)kx * g.plane + (long long)z * g.nyp + y] = make_float2(v.x * scale, v.y * scale);
+}
+
+int launch_otf_full(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* full,
+                    float scale, cudaStream_t st) {
+  dim3 grid(ceil_div(g.ny, 128), g.nz, g.nxh);
+  k_otf_full<<<grid, 128, 0, st>>>(g, od.nx_otf, od.ny_otf, od.nz_otf, od.kxscale, od.kyscale,
+                                   od.kzscale, raw_otf, full, scale);
+  CDX_LAUNCH_CHECK("k_otf_full");
+  return 0;
+}
+
+}  // namespace cdx

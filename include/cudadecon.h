@@ -1,0 +1,167 @@
+/*
+ * cudadecon_gb300 C ABI.
+ *
+ * The first block keeps the exported entry points of the reference library
+ * libcudaDecon (scopetools/cudadecon, src/linearDecon.h:243-317) with the same
+ * names, argument order, argument meaning and return convention (1 = success,
+ * 0 = failure), so that a ctypes caller such as pycudadecon can load this
+ * library in its place.  Unlike the reference, no entry point exits the
+ * process or throws across the ABI on a CUDA error: it returns 0 and the
+ * reason is available from cdx_last_error().
+ *
+ * The second block adds entry points with no counterpart in the reference:
+ * the same RL pipeline on device pointers and a caller stream, the geometry
+ * kernels on device pointers, and FFT test hooks.
+ */
+#ifndef CUDADECON_GB300_H
+#define CUDADECON_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+#define CDX_DEFAULT(v) = v
+extern "C" {
+#else
+#include <stdbool.h>
+#define CDX_DEFAULT(v)
+#endif
+
+/* ------------------------------------------------------------------ *
+ * Reference ABI                                                       *
+ * ------------------------------------------------------------------ */
+
+/* Replaces RL_interface_init (src/linearDecon.h:260-264, defined at
+ * src/RL-Biggs-Andrews.cpp:531-655).  Rounds ny, nz (and nx when there is
+ * no deskew) down to 2,3,5,7-smooth sizes, loads the OTF file (TIFF or .cimg),
+ * derives the deskew factor / deskewed width / rotation matrix and prepares
+ * the FFT plans and the OTF table for the decon grid.  Returns 0 when the OTF
+ * cannot be read or a size is unsupported. */
+int RL_interface_init(int nx, int ny, int nz, float dr, float dz, float dr_psf, float dz_psf,
+                      float deskewAngle, float rotationAngle, int outputWidth, bool bSkewedDecon,
+                      char* OTF_file_name);
+
+/* Replaces RL_interface (src/linearDecon.h:278-283, defined at
+ * src/RL-Biggs-Andrews.cpp:657-705): crop at the origin to the init sizes,
+ * apodize, subtract background, optional bleach rescale, deskew, z blend,
+ * optional mirrored stack, nIters Biggs-Andrews RL iterations, optional
+ * deskew after decon and rotation.  result must hold
+ * get_output_nx()*get_output_ny()*get_output_nz() floats. */
+int RL_interface(const unsigned short* const raw_data, int nx, int ny, int nz, float* result,
+                 float* raw_deskewed_result, float background, bool bDoRescale,
+                 bool bSaveDeskewedRaw, int nIters, int extraShift, int napodize CDX_DEFAULT(0),
+                 int nZblend CDX_DEFAULT(0), float padVal CDX_DEFAULT(0),
+                 bool bDupRevStack CDX_DEFAULT(false), bool bSkewedDecon CDX_DEFAULT(false));
+
+/* Replaces Deskew_interface (src/linearDecon.h:285-288, defined at
+ * src/RL-Biggs-Andrews.cpp:724-773), including its output width rule when
+ * outputWidth == 0 (uses the nz of the last RL_interface_init, divided by 4). */
+int Deskew_interface(const float* const raw_data, int nx, int ny, int nz, float dz, float dr,
+                     float deskewAngle, float* const result, int outputWidth, int extraShift,
+                     float padVal CDX_DEFAULT(0));
+
+/* Replaces Affine_interface (src/linearDecon.h:290-292; RL-Biggs-Andrews.cpp:776-814
+ * and geometryTransform.cu:183-213,257-301): out(x,y,z) = trilinear sample of
+ * the input at M*(x,y,z,1) with border 0; M is a 4x4 row-major matrix. */
+int Affine_interface(const float* const raw_data, int nx, int ny, int nz, float* const result,
+                     const float* affMat);
+
+/* Replaces Affine_interface_RA (src/linearDecon.h:294-296; RL-Biggs-Andrews.cpp:816-855
+ * and geometryTransform.cu:216-253,304-349): the same in world coordinates with
+ * voxel size (dx, dy, dz). */
+int Affine_interface_RA(const float* const raw_data, int nx, int ny, int nz, float dx, float dy,
+                        float dz, float* const result, const float* affMat);
+
+/* Replaces camcor_interface_init (declared at src/linearDecon.h:298-299; the
+ * reference's only definition, src/llspy.cpp:70-78, is not built).  camparam
+ * holds three nx*ny float planes: a, b, offset (camcor.cu:97-99). */
+int camcor_interface_init(int nx, int ny, int nz, const float* const camparam);
+
+/* Replaces camcor_interface (declared at src/linearDecon.h:301-303; semantics
+ * of camcor_kernel, src/camcor.cu:80-108). */
+int camcor_interface(const unsigned short* const raw_data, int nx, int ny, int nz,
+                     unsigned short* const result);
+
+/* Replaces RL_cleanup (src/linearDecon.h:306; RL-Biggs-Andrews.cpp:707-715):
+ * frees the OTF, plans and buffers and resets the bleach-correction state. */
+void RL_cleanup(void);
+
+/* Replaces cuda_reset (src/linearDecon.h:307; RL-Biggs-Andrews.cpp:717-720). */
+void cuda_reset(void);
+
+/* Replace get_output_nx/ny/nz (src/linearDecon.h:311-313;
+ * RL-Biggs-Andrews.cpp:474-503), including the reference's use of the signed
+ * rotation-matrix entry in get_output_nx. */
+unsigned get_output_nx(void);
+unsigned get_output_ny(void);
+unsigned get_output_nz(void);
+
+/* Replaces get_version (src/linearDecon.h:316). */
+const char* get_version(void);
+
+/* ------------------------------------------------------------------ *
+ * Extensions (no counterpart in the reference)                        *
+ * ------------------------------------------------------------------ */
+
+/* Message of the last failure of any entry point ("" when none). */
+const char* cdx_last_error(void);
+
+/* RL_interface on device memory and a caller stream (cudaStream_t, may be
+ * NULL for the legacy default stream).  raw_data (u16), result and
+ * raw_deskewed_result are device pointers.  Work buffers are owned by the
+ * library and reused across calls; the call returns once all work is
+ * enqueued (it synchronises only when bDoRescale needs the bleach statistic
+ * on the host). */
+int cdx_RL_device(const unsigned short* raw_data, int nx, int ny, int nz, float* result,
+                  float* raw_deskewed_result, float background, bool bDoRescale,
+                  bool bSaveDeskewedRaw, int nIters, int extraShift, int napodize, int nZblend,
+                  float padVal, bool bDupRevStack, bool bSkewedDecon, void* stream);
+
+/* Sizes of the decon grid (the volume the RL iterations run on) of the
+ * current RL_interface_init session. */
+int cdx_decon_grid(int* nx, int* ny, int* nz);
+
+/* Number of kernels the last cdx_RL_device / RL_interface call launched. */
+long long cdx_last_launch_count(void);
+
+/* Per-pass timing of the RL iteration with CUDA events recorded on the launch
+ * stream.  cdx_profile_enable(1) resets the accumulators and starts
+ * recording; cdx_profile_read synchronises and returns the number of passes
+ * per iteration (9), the summed milliseconds and counts of each pass, and of
+ * whole iterations.  cdx_profile_pass_name(i) names pass i. */
+int cdx_profile_enable(int on);
+int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, double* iter_ms,
+                     long long* iter_count);
+const char* cdx_profile_pass_name(int i);
+
+/* Deskew / rotate / camcor on device pointers (same arithmetic as the
+ * reference kernels).  rot is a host pointer to the 4 rotation-matrix floats. */
+int cdx_deskew_device(const float* in, int nx, int ny, int nz, double deskewFactor, float* out,
+                      int nxOut, int extraShift, float padVal, void* stream);
+int cdx_rotate_device(const float* in, int nx, int ny, int nz, const float* rot, float* out,
+                      int nx_out, int nz_out, void* stream);
+int cdx_camcor_device(const unsigned short* raw, int nx, int ny, int nz, const float* camparam,
+                      unsigned short* out, void* stream);
+
+/* FFT test hooks on device pointers: forward 3D real FFT of in (nz, ny, nx)
+ * written in numpy/cuFFT order (nz, ny, nx/2+1) complex64; and the
+ * convolution out = irfftn(rfftn(in) * H) where H is the OTF of the current
+ * RL_interface_init session evaluated on the (nx, ny, nz) grid (conj != 0
+ * uses conj(H)). */
+int cdx_rfft3d_device(const float* in, void* out_complex, int nx, int ny, int nz, void* stream);
+int cdx_conv3d_device(const float* in, float* out, int nx, int ny, int nz, int conj, void* stream);
+
+/* 1 if n is a product of 2, 3, 5 and 7 (a supported FFT length). */
+int cdx_fft_length_supported(int n);
+
+/* Read an image file (TIFF or .cimg) the way RL_interface_init reads the
+ * OTF.  Writes the CImg sizes (width, height, depth) and, when out is not
+ * NULL and capacity (in floats) suffices, the samples in CImg order.
+ * Returns 1 on success.  Host only: usable without a GPU. */
+int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
+                   size_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUDADECON_GB300_H */
