@@ -63,7 +63,22 @@ int fft_len_init(FftLen& f, int L) {
   }
   f.dev.L = L;
   f.dev.nst = (rad.size() == 1 && rad[0] == 1) ? 0 : (int)rad.size();
-  for (int i = 0; i < kMaxStages; ++i) f.dev.radix[i] = i < (int)rad.size() ? rad[i] : 1;
+  int Ns = 1;
+  for (int i = 0; i < kMaxStages; ++i) {
+    StageDev& sd = f.dev.st[i];
+    if (i < f.dev.nst) {
+      const int R = rad[i];
+      sd.R = R;
+      sd.LR = L / R;
+      sd.Ns = Ns;
+      sd.tws = L / (Ns * R);
+      sd.invLR = 1.0f / (float)sd.LR;
+      sd.invNs = 1.0f / (float)Ns;
+      Ns *= R;
+    } else {
+      sd = StageDev{1, L, Ns, 1, 1.0f / (float)L, 1.0f / (float)Ns};
+    }
+  }
   std::vector<float2> tw(L);
   const double two_pi = 6.283185307179586476925286766559;
   for (int m = 0; m < L; ++m) {
@@ -116,8 +131,22 @@ static int threads_for(long long elems) {
   return (int)t;
 }
 
-// Store the packed-row FFT held in sm (P vectors of length nx) into S.
-__device__ __forceinline__ void store_half_spectra(const Geom& g, const float2* sm, int P, int z,
+// Bytes of dynamic shared memory: twiddles + padded tile (+ extra float2s).
+static size_t fft_smem(int L, long long tile, long long extra = 0) {
+  return sizeof(float2) * ((size_t)L + spad_size((int)tile) + (size_t)extra);
+}
+
+// Allow a kernel the dynamic shared memory it is launched with (the default
+// limit is 48 KB; long rows need more).
+template <class K>
+static int smem_optin(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return 0;
+  CDX_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return 0;
+}
+
+// Store the packed-row FFT held in the tile (P vectors of length nx) into S.
+__device__ __forceinline__ void store_half_spectra(const Geom& g, const SmemIO& io, int P, int z,
                                                    int y0, float2* S) {
   const int nx = g.nx;
   for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
@@ -125,17 +154,17 @@ __device__ __forceinline__ void store_half_spectra(const Geom& g, const float2* 
     const int k = idx / P;
     const int ya = y0 + 2 * p;
     if (ya >= g.ny) continue;
-    const float2 zk = sm[p * nx + k];
-    const float2 zm = sm[p * nx + (k == 0 ? 0 : nx - k)];
-    float4 v = split_pair(zk, zm);
-    *reinterpret_cast<float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya) = v;
+    const float2 zk = io.ld(p, k);
+    const float2 zm = io.ld(p, k == 0 ? 0 : nx - k);
+    *reinterpret_cast<float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya) =
+        split_pair(zk, zm);
   }
 }
 
 // Load the two half spectra of rows (ya, ya+1) and rebuild the packed
-// full-length spectrum Z = A + iB in sm.  The imaginary parts of the DC and
-// (even nx) Nyquist bins are dropped, as a C2R transform does.
-__device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2* S, float2* sm,
+// full-length spectrum Z = A + iB in the tile.  The imaginary parts of the
+// DC and (even nx) Nyquist bins are dropped, as a C2R transform does.
+__device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2* S, const SmemIO& io,
                                                     int P, int z, int y0) {
   const int nx = g.nx;
   for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
@@ -150,40 +179,246 @@ __device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2*
       v.w = 0.f;
     }
     // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
-    sm[p * nx + k] = make_float2(v.x - v.w, v.y + v.z);
-    if (k > 0 && 2 * k != nx) sm[p * nx + nx - k] = make_float2(v.x + v.w, v.z - v.y);
+    io.st(p, k, make_float2(v.x - v.w, v.y + v.z));
+    if (k > 0 && 2 * k != nx) io.st(p, nx - k, make_float2(v.x + v.w, v.z - v.y));
   }
 }
 
-// ---------------------------------------------------------------- x forward
-__global__ void __launch_bounds__(kMaxThreads, 1) k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X,
-                        const float* __restrict__ Xm1, const float* __restrict__ lamp, int predict,
-                        float2* __restrict__ S, int P) {
-  extern __shared__ float2 sm[];
-  const int z = blockIdx.y;
-  const int y0 = blockIdx.x * 2 * P;
-  const int nx = g.nx;
-  const float lam = predict ? __ldg(lamp) : 0.f;
-  const long long zoff = (long long)z * g.ny * nx;
-  for (int idx = threadIdx.x; idx < P * nx; idx += blockDim.x) {
-    const int p = idx / nx;
-    const int n = idx - p * nx;
-    const int ya = y0 + 2 * p;
+// ---------------------------------------------------------------- stage I/O
+// Outputs per load batch of the fused epilogues (bounds their registers).
+constexpr int kStoreBatch = 4;
+
+// First-stage loader of the forward x pass: row pair v of the tile (rows
+// y0+2v and y0+2v+1 of slice z) packed as a + i b, with the prediction
+// Y = max(X + lambda (X - X_{k-1}), 0) applied on the fly when predict != 0.
+struct RowPairLoad {
+  static constexpr bool kSmem = false;
+  static constexpr bool kGroup = false;
+  const float* X;
+  const float* Xm1;
+  float lam;
+  int predict;
+  long long zoff;
+  int y0, ny, nx;
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    const int ya = y0 + 2 * v;
     float a = 0.f, b = 0.f;
-    if (ya < g.ny) {
-      const long long o = zoff + (long long)ya * nx + n;
+    if (ya < ny) {
+      const long long o = zoff + (long long)ya * nx + e;
       a = __ldg(X + o);
       if (predict) a = predict_y(a, __ldg(Xm1 + o), lam);
-      if (ya + 1 < g.ny) {
+      if (ya + 1 < ny) {
         b = __ldg(X + o + nx);
         if (predict) b = predict_y(b, __ldg(Xm1 + o + nx), lam);
       }
     }
-    sm[idx] = make_float2(a, b);
+    return make_float2(a, b);
   }
+};
+
+// Rows r0 + v of the spectrum (one (kx, z) row of length ny each).
+struct SpecRowIO {
+  static constexpr bool kSmem = false;
+  static constexpr bool kGroup = false;
+  float2* S;
+  long long r0, nrows;
+  int nyp;
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    const long long r = r0 + v;
+    return r < nrows ? S[r * nyp + e] : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const {
+    const long long r = r0 + v;
+    if (r < nrows) S[r * nyp + e] = x;
+  }
+};
+
+// Columns y0 + v of one kx plane of the spectrum, element e = z.
+struct SpecColIO {
+  static constexpr bool kSmem = false;
+  static constexpr bool kGroup = false;
+  float2* base;
+  int y0, ny, nyp;
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    const int y = y0 + v;
+    return y < ny ? base[(long long)e * nyp + y] : make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const {
+    const int y = y0 + v;
+    if (y < ny) base[(long long)e * nyp + y] = x;
+  }
+};
+
+// Last forward z stage: multiply by the OTF tile and store to shared memory.
+struct OtfMulStore {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  SmemIO io;
+  const float2* otf;  // [e * W + v]
+  int W, conj;
+  __device__ __forceinline__ void st(int v, int e, float2 x) const {
+    const float2 o = otf[e * W + v];
+    io.st(v, e, conj ? cmulconj(x, o) : cmul(x, o));
+  }
+};
+
+// Last inverse x stage of the first convolution: the RL ratio of the
+// reference's LRcore_kernel (RLgpuImpl.cu:416-434) for both rows of pair v,
+// written to the tile for the forward transform that follows.
+__device__ __forceinline__ float rl_ratio(float c, float raw, float eps) {
+  float v = fabsf(c) > 0.f ? c : eps;
+  v = __fadd_rn(__fdiv_rn(raw, v), eps);
+  v = v > 10.f ? 10.f : v;
+  v = v < -10.f ? -10.f : v;
+  return v;
+}
+
+struct RatioStore {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = true;
+  SmemIO io;
+  const float* raw;
+  long long zoff;
+  int y0, ny, nx;
+  float eps;
+  template <int R>
+  __device__ __forceinline__ void st_group(int v, int base, int stride, const float2* c) const {
+    const int ya = y0 + 2 * v;
+    const bool va = ya < ny, vb = ya + 1 < ny;
+    const long long o = zoff + (long long)ya * nx;
+    constexpr int C = R < kStoreBatch ? R : kStoreBatch;
+#pragma unroll
+    for (int q0 = 0; q0 < R; q0 += C) {
+      // the last batch of a radix that is not a multiple of C is partial
+      float ra[C], rb[C];
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        ra[q] = 0.f;
+        rb[q] = 0.f;
+        if (q0 + q < R) {
+          const int e = base + (q0 + q) * stride;
+          if (va) ra[q] = __ldg(raw + o + e);
+          if (vb) rb[q] = __ldg(raw + o + nx + e);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        if (q0 + q < R) {
+          const float2 r = make_float2(va ? rl_ratio(c[q0 + q].x, ra[q], eps) : 0.f,
+                                       vb ? rl_ratio(c[q0 + q].y, rb[q], eps) : 0.f);
+          io.st(v, base + (q0 + q) * stride, r);
+        }
+      }
+    }
+  }
+};
+
+// Last inverse x stage of the second convolution: estimate update
+// (currEstimate_kernel + currPrevDiff_kernel, RLgpuImpl.cu:462-470, 501-508)
+// with the Biggs-Andrews dot products of innerProduct_kernel
+// (RLgpuImpl.cu:571-633: float products, double sums).
+struct UpdateStore {
+  static constexpr bool kSmem = false;
+  static constexpr bool kGroup = true;
+  const float* X;
+  const float* Xm1;
+  float* Xout;
+  float* G;
+  float lam;
+  int predict, dots;
+  long long zoff;
+  int y0, ny, nx;
+  double* s1;
+  double* s2;
+  // The first n of C elements of one row at offsets o + e[q]: all loads
+  // first, then the stores.
+  template <int C>
+  __device__ __forceinline__ void rows(long long o, const int* e, const float* cc, int n) const {
+    float x[C], xm[C], go[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      x[q] = 0.f;
+      xm[q] = 0.f;
+      go[q] = 0.f;
+      if (q < n) {
+        x[q] = X[o + e[q]];
+        if (predict) xm[q] = Xm1[o + e[q]];
+        if (dots) go[q] = G[o + e[q]];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      if (q < n) {
+        const float yv = predict ? predict_y(x[q], xm[q], lam) : x[q];
+        float xn = __fmul_rn(cc[q], yv);
+        xn = xn > 0.f ? xn : 0.f;
+        const float gn = __fsub_rn(xn, yv);
+        if (dots) {
+          *s1 += (double)__fmul_rn(gn, go[q]);
+          *s2 += (double)__fmul_rn(go[q], go[q]);
+        }
+        Xout[o + e[q]] = xn;
+        G[o + e[q]] = gn;
+      }
+    }
+  }
+  template <int R>
+  __device__ __forceinline__ void st_group(int v, int base, int stride, const float2* c) const {
+    const int ya = y0 + 2 * v;
+    if (ya >= ny) return;
+    const long long o = zoff + (long long)ya * nx;
+    constexpr int C = R < kStoreBatch ? R : kStoreBatch;
+#pragma unroll
+    for (int q0 = 0; q0 < R; q0 += C) {
+      // the last batch of a radix that is not a multiple of C is partial
+      const int n = (R - q0) < C ? (R - q0) : C;
+      int e[C];
+      float ca[C], cb[C];
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        const int qq = (q0 + q < R) ? q0 + q : R - 1;  // clamp the unused lanes
+        e[q] = base + qq * stride;
+        ca[q] = c[qq].x;
+        cb[q] = c[qq].y;
+      }
+      rows<C>(o, e, ca, n);
+      if (ya + 1 < ny) rows<C>(o + nx, e, cb, n);
+    }
+  }
+};
+
+struct PlainRowStore {
+  static constexpr bool kSmem = false;
+  static constexpr bool kGroup = false;
+  float* out;
+  long long zoff;
+  int y0, ny, nx;
+  __device__ __forceinline__ void st(int v, int e, float2 c) const {
+    const int ya = y0 + 2 * v;
+    if (ya < ny) {
+      const long long o = zoff + (long long)ya * nx + e;
+      out[o] = c.x;
+      if (ya + 1 < ny) out[o + nx] = c.y;
+    }
+  }
+};
+
+// ---------------------------------------------------------------- x forward
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, const float* __restrict__ Xm1,
+        const float* __restrict__ lamp, int predict, float2* __restrict__ S, int P) {
+  extern __shared__ float2 smem[];
+  const int nx = g.nx;
+  float2* stw = smem;
+  const SmemIO io{smem + nx, 1, nx};
+  const int z = blockIdx.y;
+  const int y0 = blockIdx.x * 2 * P;
+  load_twiddles(fx, stw);
   __syncthreads();
-  fft_tile<false>(sm, fx, P, 1, nx, false);
-  store_half_spectra(g, sm, P, z, y0, S);
+  const RowPairLoad ld{X, Xm1, predict ? __ldg(lamp) : 0.f, predict, (long long)z * g.ny * nx,
+                       y0, g.ny, nx};
+  fft_run<false>(fx, P, 1.f, false, stw, io, ld, io);
+  store_half_spectra(g, io, P, z, y0, S);
 }
 
 int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* Xm1,
@@ -191,7 +426,8 @@ int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* X
   const int P = x_pairs(g.nx);
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   int T = threads_for((long long)P * g.nx);
-  size_t smem = sizeof(float2) * P * g.nx;
+  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  if (int rc = smem_optin(k_x_fwd, smem)) return rc;
   k_x_fwd<<<grid, T, smem, st>>>(g, fx.dev, X, Xm1, lam, predict, S, P);
   CDX_LAUNCH_CHECK("k_x_fwd");
   return 0;
@@ -199,26 +435,16 @@ int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* X
 
 // ---------------------------------------------------------------- y pass
 template <bool INV>
-__global__ void __launch_bounds__(kMaxThreads, 1) k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
-  extern __shared__ float2 sm[];
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
+  extern __shared__ float2 smem[];
   const int ny = g.ny;
-  const long long nrows = (long long)g.nxh * g.nz;
-  const long long r0 = (long long)blockIdx.x * V;
-  // rows r0..r0+V-1, row r at S + r*nyp (kx = r / nz, z = r % nz; plane = nz*nyp)
-  for (int idx = threadIdx.x; idx < V * ny; idx += blockDim.x) {
-    const int v = idx / ny;
-    const int e = idx - v * ny;
-    const long long r = r0 + v;
-    sm[idx] = r < nrows ? S[r * g.nyp + e] : make_float2(0.f, 0.f);
-  }
+  float2* stw = smem;
+  const SmemIO io{smem + ny, 1, ny};
+  load_twiddles(fy, stw);
   __syncthreads();
-  fft_tile<INV>(sm, fy, V, 1, ny, false);
-  for (int idx = threadIdx.x; idx < V * ny; idx += blockDim.x) {
-    const int v = idx / ny;
-    const int e = idx - v * ny;
-    const long long r = r0 + v;
-    if (r < nrows) S[r * g.nyp + e] = sm[idx];
-  }
+  const SpecRowIO gio{S, (long long)blockIdx.x * V, (long long)g.nxh * g.nz, g.nyp};
+  fft_run<INV>(fy, V, 1.f, false, stw, io, gio, gio);
 }
 
 int launch_y_pass(const Geom& g, const FftLen& fy, float2* S, bool inverse, cudaStream_t st) {
@@ -226,8 +452,9 @@ int launch_y_pass(const Geom& g, const FftLen& fy, float2* S, bool inverse, cuda
   if (V < 1) V = 1;
   const long long nrows = (long long)g.nxh * g.nz;
   int T = threads_for((long long)V * g.ny);
-  size_t smem = sizeof(float2) * V * g.ny;
+  size_t smem = fft_smem(g.ny, (long long)V * g.ny);
   dim3 grid((unsigned)((nrows + V - 1) / V));
+  if (int rc = smem_optin(inverse ? k_y_pass<true> : k_y_pass<false>, smem)) return rc;
   if (inverse)
     k_y_pass<true><<<grid, T, smem, st>>>(g, fy.dev, S, V);
   else
@@ -246,66 +473,55 @@ static int z_cols(int nz) {
   return w;
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1) k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj,
-                         int fwd_only, int W) {
-  extern __shared__ float2 sm[];
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int W) {
+  extern __shared__ float2 smem[];
+  const int nz = g.nz;
   const int kx = blockIdx.y;
   const int y0 = blockIdx.x * W;
-  const int nz = g.nz;
-  float2* base = S + (long long)kx * g.plane;
-  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-    const int w = idx % W;
-    const int z = idx / W;
-    const int y = y0 + w;
-    sm[idx] = y < g.ny ? base[(long long)z * g.nyp + y] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  fft_tile<false>(sm, fz, W, W, 1, true);
+  float2* stw = smem;
+  const SmemIO io{smem + nz, W, 1};
+  float2* otf_tile = smem + nz + spad_size(W * nz);
+  load_twiddles(fz, stw);
+  const float invW = 1.f / (float)W;
+  const SpecColIO gio{S + (long long)kx * g.plane, y0, g.ny, g.nyp};
   if (fwd_only) {
-    for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-      const int w = idx % W;
-      const int z = idx / W;
-      const int y = y0 + w;
-      if (y < g.ny) base[(long long)z * g.nyp + y] = sm[idx];
-    }
+    __syncthreads();
+    fft_run<false>(fz, W, invW, true, stw, io, gio, gio);
     return;
   }
-  // multiply by the OTF, interpolated on the fly (RA) or read (3D)
+  // OTF of every (y, z) of the tile, interpolated on the fly from the
+  // kz-resampled radial table (dev_otfinterpolate RA branch,
+  // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
+  // read from the precomputed 3D array
   for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
     const int w = idx % W;
     const int z = idx / W;
     const int y = y0 + w;
-    if (y >= g.ny) continue;
-    float2 o;
-    if (otf.mode == 1) {
-      o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
-    } else {
-      // reference dev_otfinterpolate RA branch (RLgpuImpl.cu:238-273):
-      // kr = sqrt(kx^2 + ky^2) in OTF radial samples, zero outside nr-1
-      const int ky = y > (g.ny >> 1) ? y - g.ny : y;
-      const float fx = (float)kx * otf.kxscale;
-      const float fy = (float)ky * otf.kyscale;
-      const float kr = sqrtf(fx * fx + fy * fy);
-      if (kr < (float)(otf.nr - 1)) {
-        const int ir = (int)floorf(kr);
-        const float ar = kr - (float)ir;
-        const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
-        const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
-        o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+    float2 o = make_float2(0.f, 0.f);
+    if (y < g.ny) {
+      if (otf.mode == 1) {
+        o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
       } else {
-        o = make_float2(0.f, 0.f);
+        const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+        const float fx = (float)kx * otf.kxscale;
+        const float fy = (float)ky * otf.kyscale;
+        const float kr = sqrtf(fx * fx + fy * fy);
+        if (kr < (float)(otf.nr - 1)) {
+          const int ir = (int)floorf(kr);
+          const float ar = kr - (float)ir;
+          const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
+          const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
+          o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+        }
       }
     }
-    sm[idx] = conj ? cmulconj(sm[idx], o) : cmul(sm[idx], o);
+    otf_tile[idx] = o;
   }
   __syncthreads();
-  fft_tile<true>(sm, fz, W, W, 1, true);
-  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-    const int w = idx % W;
-    const int z = idx / W;
-    const int y = y0 + w;
-    if (y < g.ny) base[(long long)z * g.nyp + y] = sm[idx];
-  }
+  const OtfMulStore ost{io, otf_tile, W, conj};
+  fft_run<false>(fz, W, invW, true, stw, io, gio, ost);
+  fft_run<true>(fz, W, invW, true, stw, io, io, gio);
 }
 
 int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf, bool conj,
@@ -313,50 +529,30 @@ int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf,
   const int W = z_cols(g.nz);
   dim3 grid(ceil_div(g.ny, W), g.nxh);
   int T = threads_for((long long)W * g.nz);
-  size_t smem = sizeof(float2) * W * g.nz;
+  size_t smem = fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
+  if (int rc = smem_optin(k_z_pass, smem)) return rc;
   k_z_pass<<<grid, T, smem, st>>>(g, fz.dev, S, otf, conj ? 1 : 0, fwd_only ? 1 : 0, W);
   CDX_LAUNCH_CHECK("k_z_pass");
   return 0;
 }
 
 // ---------------------------------------------------------------- x inverse
-__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S,
-                                  const float* __restrict__ raw, float eps, int P) {
-  extern __shared__ float2 sm[];
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __restrict__ raw,
+                  float eps, int P) {
+  extern __shared__ float2 smem[];
+  const int nx = g.nx;
+  float2* stw = smem;
+  const SmemIO io{smem + nx, 1, nx};
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
-  const int nx = g.nx;
-  load_packed_spectra(g, S, sm, P, z, y0);
+  load_twiddles(fx, stw);
+  load_packed_spectra(g, S, io, P, z, y0);
   __syncthreads();
-  fft_tile<true>(sm, fx, P, 1, nx, false);
-  // RL ratio of the reference's LRcore_kernel (RLgpuImpl.cu:416-434)
-  const long long zoff = (long long)z * g.ny * nx;
-  for (int idx = threadIdx.x; idx < P * nx; idx += blockDim.x) {
-    const int p = idx / nx;
-    const int n = idx - p * nx;
-    const int ya = y0 + 2 * p;
-    float2 c = sm[idx];
-    float2 r = make_float2(0.f, 0.f);
-    if (ya < g.ny) {
-      const long long o = zoff + (long long)ya * nx + n;
-      float v = fabsf(c.x) > 0.f ? c.x : eps;
-      v = __fadd_rn(__fdiv_rn(__ldg(raw + o), v), eps);
-      v = v > 10.f ? 10.f : v;
-      v = v < -10.f ? -10.f : v;
-      r.x = v;
-      if (ya + 1 < g.ny) {
-        float u = fabsf(c.y) > 0.f ? c.y : eps;
-        u = __fadd_rn(__fdiv_rn(__ldg(raw + o + nx), u), eps);
-        u = u > 10.f ? 10.f : u;
-        u = u < -10.f ? -10.f : u;
-        r.y = u;
-      }
-    }
-    sm[idx] = r;
-  }
-  __syncthreads();
-  fft_tile<false>(sm, fx, P, 1, nx, false);
-  store_half_spectra(g, sm, P, z, y0, S);
+  const RatioStore rs{io, raw, (long long)z * g.ny * nx, y0, g.ny, nx, eps};
+  fft_run<true>(fx, P, 1.f, false, stw, io, io, rs);
+  fft_run<false>(fx, P, 1.f, false, stw, io, io, io);
+  store_half_spectra(g, io, P, z, y0, S);
 }
 
 int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const float* raw,
@@ -364,7 +560,8 @@ int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const flo
   const int P = x_pairs(g.nx);
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   int T = threads_for((long long)P * g.nx);
-  size_t smem = sizeof(float2) * P * g.nx;
+  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  if (int rc = smem_optin(k_x_inv_ratio_fwd, smem)) return rc;
   k_x_inv_ratio_fwd<<<grid, T, smem, st>>>(g, fx.dev, S, raw, eps, P);
   CDX_LAUNCH_CHECK("k_x_inv_ratio_fwd");
   return 0;
@@ -394,44 +591,26 @@ __device__ __forceinline__ void block_sum2(double& a, double& b, double* red) {
   }
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S,
-                               const float* __restrict__ X, const float* Xm1,
-                               const float* __restrict__ lamp, int predict, float* Xout,
-                               float* __restrict__ G, int dots, double* partials,
-                               unsigned* counter, float* lam_next, float eps, int P) {
-  extern __shared__ float2 sm[];
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* __restrict__ X,
+               const float* Xm1, const float* __restrict__ lamp, int predict, float* Xout,
+               float* __restrict__ G, int dots, double* partials, unsigned* counter,
+               float* lam_next, float eps, int P) {
+  extern __shared__ float2 smem[];
   __shared__ double red[64];
   __shared__ bool last;
+  const int nx = g.nx;
+  float2* stw = smem;
+  const SmemIO io{smem + nx, 1, nx};
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
-  const int nx = g.nx;
-  const float lam = predict ? __ldg(lamp) : 0.f;
-  load_packed_spectra(g, S, sm, P, z, y0);
+  load_twiddles(fx, stw);
+  load_packed_spectra(g, S, io, P, z, y0);
   __syncthreads();
-  fft_tile<true>(sm, fx, P, 1, nx, false);
-  const long long zoff = (long long)z * g.ny * nx;
   double s1 = 0.0, s2 = 0.0;
-  for (int idx = threadIdx.x; idx < 2 * P * nx; idx += blockDim.x) {
-    const int rr = idx / nx;  // row within the tile
-    const int n = idx - rr * nx;
-    const int y = y0 + rr;
-    if (y >= g.ny) continue;
-    const float2 c2 = sm[(rr >> 1) * nx + n];
-    const float cc = (rr & 1) ? c2.y : c2.x;
-    const long long o = zoff + (long long)y * nx + n;
-    const float x = X[o];
-    const float yv = predict ? predict_y(x, Xm1[o], lam) : x;
-    float xn = __fmul_rn(cc, yv);
-    xn = xn > 0.f ? xn : 0.f;
-    const float gn = __fsub_rn(xn, yv);
-    if (dots) {
-      const float go = G[o];
-      s1 += (double)__fmul_rn(gn, go);
-      s2 += (double)__fmul_rn(go, go);
-    }
-    Xout[o] = xn;
-    G[o] = gn;
-  }
+  const UpdateStore us{X, Xm1, Xout, G, predict ? __ldg(lamp) : 0.f, predict, dots,
+                       (long long)z * g.ny * nx, y0, g.ny, nx, &s1, &s2};
+  fft_run<true>(fx, P, 1.f, false, stw, io, io, us);
   if (!dots) return;
   block_sum2(s1, s2, red);
   const int nblk = gridDim.x * gridDim.y;
@@ -474,31 +653,27 @@ int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const 
     return cudaErrorInvalidValue;
   }
   int T = threads_for((long long)P * g.nx);
-  size_t smem = sizeof(float2) * P * g.nx;
+  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  if (int rc = smem_optin(k_x_inv_update, smem)) return rc;
   k_x_inv_update<<<grid, T, smem, st>>>(g, fx.dev, S, X, Xm1, lam, predict, Xout, G, dots,
                                         w.partials, w.counter, lam_next, eps, P);
   CDX_LAUNCH_CHECK("k_x_inv_update");
   return 0;
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1) k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S,
-                              float* __restrict__ out, int P) {
-  extern __shared__ float2 sm[];
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S, float* __restrict__ out, int P) {
+  extern __shared__ float2 smem[];
+  const int nx = g.nx;
+  float2* stw = smem;
+  const SmemIO io{smem + nx, 1, nx};
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
-  const int nx = g.nx;
-  load_packed_spectra(g, S, sm, P, z, y0);
+  load_twiddles(fx, stw);
+  load_packed_spectra(g, S, io, P, z, y0);
   __syncthreads();
-  fft_tile<true>(sm, fx, P, 1, nx, false);
-  const long long zoff = (long long)z * g.ny * nx;
-  for (int idx = threadIdx.x; idx < 2 * P * nx; idx += blockDim.x) {
-    const int rr = idx / nx;
-    const int n = idx - rr * nx;
-    const int y = y0 + rr;
-    if (y >= g.ny) continue;
-    const float2 c2 = sm[(rr >> 1) * nx + n];
-    out[zoff + (long long)y * nx + n] = (rr & 1) ? c2.y : c2.x;
-  }
+  const PlainRowStore ps{out, (long long)z * g.ny * nx, y0, g.ny, nx};
+  fft_run<true>(fx, P, 1.f, false, stw, io, io, ps);
 }
 
 int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* out,
@@ -506,7 +681,8 @@ int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* 
   const int P = x_pairs(g.nx);
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   int T = threads_for((long long)P * g.nx);
-  size_t smem = sizeof(float2) * P * g.nx;
+  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  if (int rc = smem_optin(k_x_inv_plain, smem)) return rc;
   k_x_inv_plain<<<grid, T, smem, st>>>(g, fx.dev, S, out, P);
   CDX_LAUNCH_CHECK("k_x_inv_plain");
   return 0;

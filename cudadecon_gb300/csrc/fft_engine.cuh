@@ -8,13 +8,17 @@
 // exp(-2*pi*i * r*(j mod Ns) / (Ns*R)), applies an R-point DFT and writes
 // output q to (j div Ns)*Ns*R + (j mod Ns) + q*Ns.
 //
-// The tile is transformed in place: in each stage every thread first pulls all
-// butterfly inputs it owns into registers, the block synchronises, and then the
-// outputs are written back.  A thread owns at most kEpt elements per stage, so
-// a tile of V vectors of length L must satisfy V*L <= blockDim.x * kEpt.
+// A stage reads the R inputs of each butterfly it owns into registers and
+// writes the R outputs; the first stage may read straight from global memory
+// and the last one may write straight to global memory (or apply a fused
+// epilogue), so a transform of s stages makes s-1 round trips through the
+// shared tile.  In-place stages synchronise between their reads and writes.
+// A thread owns at most kEpt elements per stage, so a tile of V vectors of
+// length L must satisfy V*L <= blockDim.x * kEpt.
 //
 // Twiddles come from a per-length table tw[m] = exp(-2*pi*i*m/L) computed in
-// double precision on the host and rounded once to float.
+// double precision on the host, rounded once to float and staged in shared
+// memory by each block.
 //
 // This replaces the cuFFT R2C/C2R calls of the reference
 // (src/RLgpuImpl.cu:183 and :218); it is used for the x, y and z passes of the
@@ -31,12 +35,6 @@ constexpr int kMaxThreads = 512; // FFT kernels launch at most this many threads
 // Longest transform: one vector must fit a tile of kMaxThreads * kEpt elements.
 constexpr int kMaxFftLen = kMaxThreads * kEpt;
 
-struct FftDev {
-  int L;
-  int nst;
-  int radix[kMaxStages];
-  const float2* tw;  // L entries, exp(-2*pi*i*m/L)
-};
 
 // ------------------------------------------------------------- constants
 // cos(2*pi*m/R) and sin(2*pi*m/R) for the odd radices, m = 0..R-1.
@@ -259,21 +257,73 @@ template <bool INV> struct Dft<5, INV> : DftOdd<5, INV> {};
 template <bool INV> struct Dft<7, INV> : DftOdd<7, INV> {};
 template <bool INV> struct Dft<9, INV> : DftOdd<9, INV> {};
 
+// ------------------------------------------------------------- tile I/O
+// Shared-memory tiles are padded with one element per 16 so that the strided
+// Stockham accesses (stride R or Ns elements) spread over the banks.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int spad_size(int n) { return n + (n >> 4) + 1; }
+
+// Exact floor(a / d) for 0 <= a < 2^22 from a float reciprocal of d: the
+// quotient of (a + 1/2) is at least 1/(2d) away from an integer, far more
+// than the rounding error of one multiply.
+__device__ __forceinline__ int fdiv(int a, float inv_d) {
+  return __float2int_rz(__fmul_rn((float)a + 0.5f, inv_d));
+}
+
+// Element e of vector v of a padded shared-memory tile.
+struct SmemIO {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  float2* sm;
+  int es, vs;
+  __device__ __forceinline__ float2 ld(int v, int e) const { return sm[spad(v * vs + e * es)]; }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[spad(v * vs + e * es)] = x; }
+};
+
+// Store the R outputs of one butterfly (elements base + q*stride of vector
+// v).  Storers that set kGroup receive them together so that their own
+// global loads (fused epilogues) are all issued before any store.
+template <int R, class St>
+__device__ __forceinline__ void store_group(const St& st, int v, int base, int stride,
+                                            const float2* x) {
+  if constexpr (St::kGroup) {
+    st.template st_group<R>(v, base, stride, x);
+  } else {
+#pragma unroll
+    for (int q = 0; q < R; ++q) st.st(v, base + q * stride, x[q]);
+  }
+}
+
 // ------------------------------------------------------------- one stage
-// Tile geometry: V vectors, element e of vector v at buf[v*vs + e*es].
-// vfast selects the butterfly->thread mapping: true puts consecutive threads
-// on consecutive vectors (for interleaved tiles, vs == 1), false on
-// consecutive butterflies of one vector (for contiguous vectors, es == 1).
-template <int R, bool INV>
-__device__ __forceinline__ void stockham_stage(float2* buf, int L, int Ns, int V, int es, int vs,
-                                               bool vfast, const float2* __restrict__ tw) {
+// Stage geometry, precomputed on the host: LR = L/R butterflies per vector,
+// span Ns, twiddle stride tws = L/(Ns*R), and float reciprocals for fdiv.
+struct StageDev {
+  int R, LR, Ns, tws;
+  float invLR, invNs;
+};
+
+struct FftDev {
+  int L;
+  int nst;
+  StageDev st[kMaxStages];
+  const float2* tw;  // L entries exp(-2*pi*i*m/L) in global memory
+};
+
+// One Stockham stage over V vectors.  The R inputs of every butterfly are
+// read with ld.ld(v, e), outputs written with st.st(v, e, x).  vfast puts
+// consecutive threads on consecutive vectors (interleaved tiles), otherwise
+// on consecutive butterflies of a vector.  SYNC_MID separates the reads from
+// the writes (needed when both touch the same shared tile); SYNC_END makes
+// the writes visible to the next stage.  stw is the twiddle table in smem.
+template <int R, bool INV, bool SYNC_MID, bool SYNC_END, class Ld, class St>
+__device__ __forceinline__ void stage_io(const StageDev& sd, int V, float invV, bool vfast,
+                                         const float2* stw, const Ld& ld, const St& st) {
   constexpr int NB = (kEpt + R - 1) / R;
   // Opaque copies: the butterfly indices below do not depend on the stage
-  // counter, and without this the compiler hoists the indices of every radix
-  // case out of the stage loop and keeps them all live (heavy spilling).
+  // and would otherwise be hoisted and kept live across stages.
   int tid = threadIdx.x, T = blockDim.x;
-  asm volatile("" : "+r"(tid), "+r"(T), "+r"(L), "+r"(V));
-  const int LR = L / R;
+  asm volatile("" : "+r"(tid), "+r"(T));
+  const int LR = sd.LR, Ns = sd.Ns;
   const int nbf = V * LR;
   float2 x[NB][R];
   int jj[NB], vv[NB];
@@ -281,73 +331,104 @@ __device__ __forceinline__ void stockham_stage(float2* buf, int L, int Ns, int V
   for (int i = 0; i < NB; ++i) {
     const int b = tid + i * T;
     jj[i] = -1;
+    vv[i] = 0;
     if (b < nbf) {
       int j, v;
       if (vfast) {
-        v = b % V;
-        j = b / V;
+        j = fdiv(b, invV);
+        v = b - j * V;
       } else {
-        j = b % LR;
-        v = b / LR;
+        v = fdiv(b, sd.invLR);
+        j = b - v * LR;
       }
       jj[i] = j;
       vv[i] = v;
-      const float2* src = buf + v * vs + j * es;
 #pragma unroll
-      for (int r = 0; r < R; ++r) x[i][r] = src[r * LR * es];
+      for (int r = 0; r < R; ++r) x[i][r] = ld.ld(v, j + r * LR);
     }
   }
-  __syncthreads();
+  if (SYNC_MID) __syncthreads();
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     const int j = jj[i];
     if (j >= 0) {
-      const int k = j % Ns;
+      const int k = j - fdiv(j, sd.invNs) * Ns;
       if (Ns > 1) {
-        const int step = (L / (Ns * R)) * k;
+        const int step = sd.tws * k;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          float2 w = __ldg(tw + r * step);
+          const float2 w = stw[r * step];
           x[i][r] = INV ? cmulconj(x[i][r], w) : cmul(x[i][r], w);
         }
       }
       Dft<R, INV>::run(x[i]);
-      float2* dst = buf + vv[i] * vs + ((j - k) * R + k) * es;
-#pragma unroll
-      for (int q = 0; q < R; ++q) dst[q * Ns * es] = x[i][q];
+      store_group<R>(st, vv[i], (j - k) * R + k, Ns, x[i]);
     }
   }
-  __syncthreads();
+  if (SYNC_END) __syncthreads();
 }
 
-// Transform V vectors of length f.L in place.  The plan lists its radices in
-// the fixed order 16..., {8|4|2}, 9..., 3..., 7..., 5... (see factorize()),
-// so the stages run as one homogeneous loop per radix.  (A single loop with a
-// switch on the radix makes the compiler keep every case's registers live.)
-// Caller must have synchronised after filling the tile; returns after a final
-// __syncthreads().
+template <bool INV, bool SYNC_MID, bool SYNC_END, class Ld, class St>
+__device__ __forceinline__ void stage_any(const StageDev& sd, int V, float invV, bool vfast,
+                                          const float2* stw, const Ld& ld, const St& st) {
+  switch (sd.R) {
+    case 2: stage_io<2, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 3: stage_io<3, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 4: stage_io<4, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 5: stage_io<5, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 7: stage_io<7, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 8: stage_io<8, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    case 9: stage_io<9, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+    default: stage_io<16, INV, SYNC_MID, SYNC_END>(sd, V, invV, vfast, stw, ld, st); break;
+  }
+}
+
+// Middle stages (shared tile in place) as one homogeneous loop per radix: the
+// plan lists radices in the fixed order 16..., {8|4|2}, 9..., 3..., 7..., 5...
+// (a single loop with a switch on the radix makes the compiler keep every
+// case's registers live).
 template <int R, bool INV>
-__device__ __forceinline__ int run_radix(float2* buf, const FftDev& f, int& s, int Ns, int V,
-                                         int es, int vs, bool vfast) {
-  while (s < f.nst && f.radix[s] == R) {
-    stockham_stage<R, INV>(buf, f.L, Ns, V, es, vs, vfast, f.tw);
-    Ns *= R;
+__device__ __forceinline__ void run_middle(const FftDev& f, int& s, int last, int V, float invV,
+                                           bool vfast, const float2* stw, const SmemIO& io) {
+  while (s < last && f.st[s].R == R) {
+    stage_io<R, INV, true, true>(f.st[s], V, invV, vfast, stw, io, io);
     ++s;
   }
-  return Ns;
 }
 
-template <bool INV>
-__device__ void fft_tile(float2* buf, const FftDev& f, int V, int es, int vs, bool vfast) {
-  int s = 0, Ns = 1;
-  Ns = run_radix<16, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<8, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<4, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<2, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<9, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<3, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<7, INV>(buf, f, s, Ns, V, es, vs, vfast);
-  Ns = run_radix<5, INV>(buf, f, s, Ns, V, es, vs, vfast);
+// Full transform of V vectors of length f.L.  The first stage reads with
+// ld0, the last stage writes with stL, and the stages in between work in
+// place on the shared tile io.  When stL writes shared memory the function
+// ends with a barrier; otherwise the caller decides.  Every thread of the
+// block must call it.
+template <bool INV, class Ld0, class StL>
+__device__ __forceinline__ void fft_run(const FftDev& f, int V, float invV, bool vfast,
+                                        const float2* stw, const SmemIO& io, const Ld0& ld0,
+                                        const StL& stL) {
+  const int ns = f.nst;
+  if (ns == 1) {
+    // a single stage may read and write the same rows (in place in global
+    // memory too), so its reads and writes are always separated
+    stage_any<INV, true, StL::kSmem>(f.st[0], V, invV, vfast, stw, ld0, stL);
+    return;
+  }
+  stage_any<INV, Ld0::kSmem, true>(f.st[0], V, invV, vfast, stw, ld0, io);
+  int s = 1;
+  const int last = ns - 1;
+  run_middle<16, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<8, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<4, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<2, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<9, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<3, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<7, INV>(f, s, last, V, invV, vfast, stw, io);
+  run_middle<5, INV>(f, s, last, V, invV, vfast, stw, io);
+  stage_any<INV, true, StL::kSmem>(f.st[last], V, invV, vfast, stw, io, stL);
+}
+
+// Copy the twiddle table of f into shared memory (caller synchronises).
+__device__ __forceinline__ void load_twiddles(const FftDev& f, float2* stw) {
+  for (int i = threadIdx.x; i < f.L; i += blockDim.x) stw[i] = __ldg(f.tw + i);
 }
 
 }  // namespace cdx

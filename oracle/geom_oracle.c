@@ -46,16 +46,21 @@ void oracle_deskew(const float* in, int nx, int ny, int nz, float* out, int nxOu
       }
 }
 
-void oracle_rotate(const float* in, int nx_in, int ny, int nz_in, float* out, int nx_out,
-                   int nz_out, const float* rot, int contract) {
+/* coord_mode: how r0*zc + r1*xc is contracted (0: not at all, 1: fmaf(r0, zc, r1*xc),
+ * 2: fmaf(r1, xc, r0*zc)); interp_mode likewise for each a*b + c*d of the
+ * bilinear blend (0: none, 1: first product fused, 2: second product fused). */
+void oracle_rotate_v(const float* in, int nx_in, int ny, int nz_in, float* out, int nx_out,
+                     int nz_out, const float* rot, int coord_mode, int interp_mode) {
   const size_t nxy_in = (size_t)nx_in * ny, nxy_out = (size_t)nx_out * ny;
+#define MAC2(a, b, c, d, mode) \
+  ((mode) == 1 ? fmaf((a), (b), (c) * (d)) : (mode) == 2 ? fmaf((c), (d), (a) * (b)) : (a) * (b) + (c) * (d))
   for (int zout = 0; zout < nz_out; ++zout)
     for (int yout = 0; yout < ny; ++yout)
       for (int xout = 0; xout < nx_out; ++xout) {
         const float xc = (float)((double)(unsigned)xout - nx_out / 2.);
         const float zc = (float)((double)(unsigned)zout - nz_out / 2.);
-        const float s0 = contract ? fmaf(rot[0], zc, rot[1] * xc) : rot[0] * zc + rot[1] * xc;
-        const float s1 = contract ? fmaf(rot[2], zc, rot[3] * xc) : rot[2] * zc + rot[3] * xc;
+        const float s0 = MAC2(rot[0], zc, rot[1], xc, coord_mode);
+        const float s1 = MAC2(rot[2], zc, rot[3], xc, coord_mode);
         const float zin = (float)((double)s0 + nz_in / 2.);
         const float xin = (float)((double)s1 + nx_in / 2.);
         const size_t indout = (size_t)(nz_out - 1 - zout) * nxy_out + (size_t)yout * nx_out + xout;
@@ -65,19 +70,23 @@ void oracle_rotate(const float* in, int nx_in, int ny, int nz_in, float* out, in
           const size_t i01 = i00 + 1, i10 = i00 + nxy_in, i11 = i10 + 1;
           const float xo = xin - fx, zo = zin - fz;
           const float wx = 1.0f - xo, wz = 1.0f - zo;
-          float r;
-          if (contract) {
-            const float a = fmaf(wx, in[i00], xo * in[i01]);
-            const float b = fmaf(wx, in[i10], xo * in[i11]);
-            r = fmaf(wz, a, zo * b);
-          } else {
-            r = wz * (wx * in[i00] + xo * in[i01]) + zo * (wx * in[i10] + xo * in[i11]);
-          }
-          out[indout] = r;
+          const float a = MAC2(wx, in[i00], xo, in[i01], interp_mode);
+          const float b = MAC2(wx, in[i10], xo, in[i11], interp_mode);
+          out[indout] = MAC2(wz, a, zo, b, interp_mode);
         } else {
           out[indout] = 0.f;
         }
       }
+#undef MAC2
+}
+
+/* The contraction the reference's nvcc build applies (pinned on the GPU). */
+int g_rotate_coord_mode = 2, g_rotate_interp_mode = 1;
+
+void oracle_rotate(const float* in, int nx_in, int ny, int nz_in, float* out, int nx_out,
+                   int nz_out, const float* rot, int contract) {
+  oracle_rotate_v(in, nx_in, ny, nz_in, out, nx_out, nz_out, rot,
+                  contract ? g_rotate_coord_mode : 0, contract ? g_rotate_interp_mode : 0);
 }
 
 /* float -> unsigned short as the GPU converts it: round toward zero,

@@ -102,11 +102,11 @@ RL_CASES = {
 @pytest.mark.parametrize("case", sorted(RL_CASES))
 def test_rl_interface_matches_oracle(cdx, oracle, torch_cuda, tmp_path, case):
     kw = RL_CASES[case]
-    shape = (21, 50, 64)  # nz, ny rounded down to 20, 50 (crop at the origin)
+    shape = (22, 50, 64)  # nz rounded down to 21 (crop at the origin); odd z length
     raw = synth.bead_stack(shape, n_beads=40, psf_sigma_xy=1.2, psf_sigma_z=2.0, seed=11)
     tab = synth.gaussian_otf_table(33, 20, 1.2, 2.0)
     _init(cdx, tmp_path, shape, tab)
-    assert cdx.output_shape() == (20, 50, 64)
+    assert cdx.output_shape() == (21, 50, 64)
     out = cdx.rl_decon(raw, background=100.0, **kw)
     st = _oracle_state(oracle, shape, tab)
     ref, _ = oracle.rl_interface(st, raw, background=100.0, nIters=kw.get("n_iters", 10),
@@ -236,6 +236,11 @@ def test_affine_matches_texture_trilinear(cdx, torch_cuda):
     pts = np.stack([x, y, z, np.ones_like(x)], -1).astype(np.float64) @ M.T.astype(np.float64)
     ref = _trilinear_border(a.astype(np.float64), pts[..., 0] + 0.5, pts[..., 1] + 0.5, pts[..., 2] + 0.5)
     assert np.max(np.abs(out - ref)) < 5e-3
-    # identity with RA voxel sizes reproduces the input
+    # the non-RA kernel adds half a voxel, so the identity reproduces the input
+    np.testing.assert_allclose(cdx.affine(a, np.eye(4, dtype=np.float32)), a, atol=1e-6)
+    # the RA kernel does not (geometryTransform.cu:236-248): the identity
+    # samples at voxel corners, averaging 2x2x2 neighbours with zero border
     out2 = cdx.affine_ra(a, np.eye(4, dtype=np.float32), 0.1, 0.1, 0.3)
-    np.testing.assert_allclose(out2, a, atol=1e-6)
+    ref2 = _trilinear_border(a.astype(np.float64), x.astype(np.float64), y.astype(np.float64),
+                             z.astype(np.float64))
+    assert np.max(np.abs(out2 - ref2)) < 5e-3
