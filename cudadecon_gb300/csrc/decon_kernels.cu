@@ -63,6 +63,8 @@ int fft_len_init(FftLen& f, int L) {
   }
   f.dev.L = L;
   f.dev.nst = (rad.size() == 1 && rad[0] == 1) ? 0 : (int)rad.size();
+  std::vector<float2> tw(L, make_float2(1.f, 0.f));
+  const double two_pi = 6.283185307179586476925286766559;
   int Ns = 1;
   for (int i = 0; i < kMaxStages; ++i) {
     StageDev& sd = f.dev.st[i];
@@ -71,19 +73,18 @@ int fft_len_init(FftLen& f, int L) {
       sd.R = R;
       sd.LR = L / R;
       sd.Ns = Ns;
-      sd.tws = L / (Ns * R);
+      sd.toff = Ns - 1;
       sd.invLR = 1.0f / (float)sd.LR;
       sd.invNs = 1.0f / (float)Ns;
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < Ns; ++k) {
+          const double a = -two_pi * (double)r * (double)k / ((double)Ns * R);
+          tw[sd.toff + (r - 1) * Ns + k] = make_float2((float)cos(a), (float)sin(a));
+        }
       Ns *= R;
     } else {
-      sd = StageDev{1, L, Ns, 1, 1.0f / (float)L, 1.0f / (float)Ns};
+      sd = StageDev{1, L, Ns, 0, 1.0f / (float)L, 1.0f / (float)Ns};
     }
-  }
-  std::vector<float2> tw(L);
-  const double two_pi = 6.283185307179586476925286766559;
-  for (int m = 0; m < L; ++m) {
-    const double a = -two_pi * (double)m / (double)L;
-    tw[m] = make_float2((float)cos(a), (float)sin(a));
   }
   CDX_CHECK(cudaMalloc(&f.d_tw, sizeof(float2) * L));
   CDX_CHECK(cudaMemcpy(f.d_tw, tw.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
@@ -117,6 +118,7 @@ __device__ __forceinline__ float4 split_pair(float2 zk, float2 zm) {
 static int x_pairs(int nx) {
   int p = (kMaxThreads * kEpt) / nx;
   if (p > 8) p = 8;
+  if (nx >= 512 && p > 4) p = 4;  // long rows: smaller tiles, more resident blocks
   if (p < 1) p = 1;
   return p;
 }
@@ -140,6 +142,8 @@ static size_t fft_smem(int L, long long tile, long long extra = 0) {
 // limit is 48 KB; long rows need more).
 template <class K>
 static int smem_optin(K kernel, size_t bytes) {
+  // prefer the largest shared-memory carveout so that several tiles fit an SM
+  CDX_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   if (bytes <= 48 * 1024) return 0;
   CDX_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return 0;

@@ -16,9 +16,8 @@
 // A thread owns at most kEpt elements per stage, so a tile of V vectors of
 // length L must satisfy V*L <= blockDim.x * kEpt.
 //
-// Twiddles come from a per-length table tw[m] = exp(-2*pi*i*m/L) computed in
-// double precision on the host, rounded once to float and staged in shared
-// memory by each block.
+// Twiddles come from per-stage tables computed in double precision on the
+// host, rounded once to float and staged in shared memory by each block.
 //
 // This replaces the cuFFT R2C/C2R calls of the reference
 // (src/RLgpuImpl.cu:183 and :218); it is used for the x, y and z passes of the
@@ -296,9 +295,9 @@ __device__ __forceinline__ void store_group(const St& st, int v, int base, int s
 
 // ------------------------------------------------------------- one stage
 // Stage geometry, precomputed on the host: LR = L/R butterflies per vector,
-// span Ns, twiddle stride tws = L/(Ns*R), and float reciprocals for fdiv.
+// span Ns, the offset of the stage's twiddles, and float reciprocals for fdiv.
 struct StageDev {
-  int R, LR, Ns, tws;
+  int R, LR, Ns, toff;  // toff: offset of this stage's twiddles in the table
   float invLR, invNs;
 };
 
@@ -306,7 +305,11 @@ struct FftDev {
   int L;
   int nst;
   StageDev st[kMaxStages];
-  const float2* tw;  // L entries exp(-2*pi*i*m/L) in global memory
+  // Per-stage twiddles in global memory: stage s with radix R and span Ns
+  // holds w[toff + (r-1)*Ns + k] = exp(-2*pi*i*r*k/(Ns*R)), r = 1..R-1,
+  // k = 0..Ns-1, so threads with consecutive k read consecutive words.  The
+  // stages together hold L-1 entries (sum of (R-1)*Ns telescopes).
+  const float2* tw;
 };
 
 // One Stockham stage over V vectors.  The R inputs of every butterfly are
@@ -354,10 +357,10 @@ __device__ __forceinline__ void stage_io(const StageDev& sd, int V, float invV, 
     if (j >= 0) {
       const int k = j - fdiv(j, sd.invNs) * Ns;
       if (Ns > 1) {
-        const int step = sd.tws * k;
+        const float2* tw = stw + sd.toff + k;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          const float2 w = stw[r * step];
+          const float2 w = tw[(r - 1) * Ns];
           x[i][r] = INV ? cmulconj(x[i][r], w) : cmul(x[i][r], w);
         }
       }
