@@ -99,6 +99,8 @@ def _bind(L) -> None:
         "cdx_rfft3d_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p]),
         "cdx_conv3d_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
         "cdx_fft_length_supported": (c_int, [c_int]),
+        "cdx_accel_factor_device": (c_int, [c_void_p, c_void_p, c_longlong, c_void_p, c_void_p,
+                                            c_void_p]),
         "cdx_load_image": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), POINTER(c_int), _F,
                                    c_size_t]),
     }

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/cudadecon.h"
+#include "accel.cuh"
 #include "kernels.h"
 #include "otf_io.h"
 
@@ -128,6 +129,9 @@ struct Session {
   DevBuf<float> lam;
   cudaStream_t stream = nullptr;
   long long launches = 0;
+  // acceleration-factor scratch (per-block partials and the last-block ticket)
+  DevBuf<double> acc_part;
+  DevBuf<unsigned> acc_cnt;
   // camcor context
   int cc_nx = 0, cc_ny = 0, cc_nz = 0;
   DevBuf<float> cc_param;
@@ -212,6 +216,8 @@ static void release_all(Session& s) {
   s.cc_param.release();
   s.cc_in.release();
   s.cc_out.release();
+  s.acc_part.release();
+  s.acc_cnt.release();
   if (s.stream) cudaStreamDestroy(s.stream);
   s.stream = nullptr;
 }
@@ -917,6 +923,26 @@ int Affine_interface_RA(const float* const raw_data, int nx, int ny, int nz, flo
 }
 
 int cdx_fft_length_supported(int n) { return fft_len_supported(n) ? 1 : 0; }
+
+int cdx_accel_factor_device(const float* g_new, const float* g_old, long long n, double* out,
+                            float* lam, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!g_new || !g_old || n < 1) {
+    set_error("cdx_accel_factor_device", "null pointer or empty array");
+    return 0;
+  }
+  const size_t nblk = (size_t)accel_blocks(n);
+  const bool fresh = s.acc_cnt.p == nullptr;
+  if (s.acc_part.ensure(2 * nblk) || s.acc_cnt.ensure(1)) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (fresh && cudaMemsetAsync(s.acc_cnt.p, 0, sizeof(unsigned), st) != cudaSuccess) {
+    set_error("cdx_accel_factor_device", "memset failed");
+    return 0;
+  }
+  const float eps = 1.1920928955078125e-07f;
+  return launch_accel_factor(g_new, g_old, n, s.acc_part.p, s.acc_cnt.p, eps, out, lam, st) == 0;
+}
 
 int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
                    size_t capacity) {

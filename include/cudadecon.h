@@ -150,6 +150,17 @@ int cdx_camcor_device(const unsigned short* raw, int nx, int ny, int nz, const f
 int cdx_rfft3d_device(const float* in, void* out_complex, int nx, int ny, int nz, void* stream);
 int cdx_conv3d_device(const float* in, float* out, int nx, int ny, int nz, int conj, void* stream);
 
+/* Biggs-Andrews acceleration factor of two device float arrays of n
+ * elements, as the reference's calcAccelFactor (src/RLgpuImpl.cu:510-569):
+ * num = g_new.g_old, den = g_old.g_old (float products, double sums),
+ * lambda = num / (den + FLT_EPSILON).  Results stay on the device: out
+ * (3 doubles, may be NULL) receives num, den and lambda; lam (1 float, may be
+ * NULL) receives lambda clamped to [0, 1] as RL-Biggs-Andrews.cpp:298 uses it.
+ * Scratch for the per-block partials is allocated by the library on first
+ * use (cudaMalloc) and reused. */
+int cdx_accel_factor_device(const float* g_new, const float* g_old, long long n, double* out,
+                            float* lam, void* stream);
+
 /* 1 if n is a product of 2, 3, 5 and 7 (a supported FFT length). */
 int cdx_fft_length_supported(int n);
 

@@ -244,3 +244,27 @@ def test_affine_matches_texture_trilinear(cdx, torch_cuda):
     ref2 = _trilinear_border(a.astype(np.float64), x.astype(np.float64), y.astype(np.float64),
                              z.astype(np.float64))
     assert np.max(np.abs(out2 - ref2)) < 5e-3
+
+
+# ---------------------------------------------------------------- acceleration factor
+@pytest.mark.parametrize("n", [1, 1000, 8192, 8193, 19353600])
+def test_accel_factor_matches_reference_formula(cdx, torch_cuda, n):
+    torch = torch_cuda
+    rng = np.random.default_rng(n)
+    g1 = rng.standard_normal(n).astype(np.float32)
+    g2 = (0.8 * g1 + 0.3 * rng.standard_normal(n)).astype(np.float32)
+    d1, d2 = _dev(torch, g1), _dev(torch, g2)
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    lam = torch.zeros(1, dtype=torch.float32, device="cuda")
+    for _ in range(2):  # the scratch is reused
+        ok = cdx.lib().cdx_accel_factor_device(ctypes.c_void_p(d1.data_ptr()), ctypes.c_void_p(d2.data_ptr()),
+                                               n, ctypes.c_void_p(out.data_ptr()),
+                                               ctypes.c_void_p(lam.data_ptr()), _stream(torch))
+        assert ok == 1
+        o = out.cpu().numpy()
+        num = np.sum((g1 * g2).astype(np.float32), dtype=np.float64)
+        den = np.sum((g2 * g2).astype(np.float32), dtype=np.float64)
+        np.testing.assert_allclose(o[:2], [num, den], rtol=1e-12)
+        l = num / (den + np.finfo(np.float32).eps)
+        np.testing.assert_allclose(o[2], l, rtol=1e-12)
+        assert lam.item() == np.float32(min(max(l, 0.0), 1.0))
