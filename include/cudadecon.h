@@ -161,6 +161,20 @@ int cdx_conv3d_device(const float* in, float* out, int nx, int ny, int nz, int c
 int cdx_accel_factor_device(const float* g_new, const float* g_old, long long n, double* out,
                             float* lam, void* stream);
 
+/* Same result as cdx_accel_factor_device, but allocates nothing: no entry
+ * point of the reference corresponds to it.  For callers that cannot let a
+ * library allocate device memory while they run -- pipelines that overlap
+ * transfers and deconvolution on several streams (cudaMalloc and cudaFree
+ * synchronise the device) and processes that reserve GPU memory up front.
+ * The scratch is a fixed 64 KB array in device memory held by every GPU that
+ * loads the library; n is limited to 33554432 elements (larger n returns 0
+ * with an error message).  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current, so make it
+ * before any stream capture.  All calls share the array and clear its counter
+ * on entry: calls that may overlap on the GPU race and must be serialised. */
+int cdx_accel_factor_device_noalloc(const float* g_new, const float* g_old, long long n,
+                                    double* out, float* lam, void* stream);
+
 /* 1 if n is a product of 2, 3, 5 and 7 (a supported FFT length). */
 int cdx_fft_length_supported(int n);
 
