@@ -171,21 +171,74 @@ __device__ __forceinline__ void store_half_spectra(const Geom& g, const SmemIO& 
 __device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2* S, const SmemIO& io,
                                                     int P, int z, int y0) {
   const int nx = g.nx;
-  for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
-    const int p = idx % P;
-    const int k = idx / P;
-    const int ya = y0 + 2 * p;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (ya < g.ny)
-      v = *reinterpret_cast<const float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya);
-    if (k == 0 || 2 * k == nx) {
-      v.y = 0.f;
-      v.w = 0.f;
+  const int n = g.nxh * P;
+  const int T = blockDim.x;
+  constexpr int B = 8;  // loads issued before the first shared store
+  for (int base = threadIdx.x; base < n; base += B * T) {
+    float4 v[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int idx = base + b * T;
+      const int p = idx % P;
+      const int k = idx / P;
+      const int ya = y0 + 2 * p;
+      v[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (idx < n && ya < g.ny)
+        v[b] = __ldg(reinterpret_cast<const float4*>(S + (long long)k * g.plane +
+                                                     (long long)z * g.nyp + ya));
     }
-    // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
-    io.st(p, k, make_float2(v.x - v.w, v.y + v.z));
-    if (k > 0 && 2 * k != nx) io.st(p, nx - k, make_float2(v.x + v.w, v.z - v.y));
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int idx = base + b * T;
+      if (idx >= n) break;
+      const int p = idx % P;
+      const int k = idx / P;
+      float4 w = v[b];
+      if (k == 0 || 2 * k == nx) {
+        w.y = 0.f;
+        w.w = 0.f;
+      }
+      // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
+      io.st(p, k, make_float2(w.x - w.w, w.y + w.z));
+      if (k > 0 && 2 * k != nx) io.st(p, nx - k, make_float2(w.x + w.w, w.z - w.y));
+    }
   }
+}
+
+// ---------------------------------------------------------------- async row copies
+// Rows y0 .. y0+nr-1 of one z slice are contiguous (nr*nx floats); they are
+// copied into shared memory with cp.async at the start of an x kernel, so
+// the copy overlaps the transform without occupying registers, and the
+// fused epilogue later reads them from shared memory.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Copy count floats from src (global) to dst (shared); 16-byte copies when
+// both addresses allow them, 4-byte copies otherwise.
+__device__ __forceinline__ void prefetch_floats(float* dst, const float* src, int count) {
+  if (((reinterpret_cast<unsigned long long>(src) | reinterpret_cast<unsigned long long>(dst)) &
+       15) == 0) {
+    const int n4 = count >> 2;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) cp_async16(dst + 4 * i, src + 4 * i);
+    for (int i = 4 * n4 + threadIdx.x; i < count; i += blockDim.x) cp_async4(dst + i, src + i);
+  } else {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) cp_async4(dst + i, src + i);
+  }
+}
+
+// Shared float2 offset after the twiddles and the padded tile of an x kernel,
+// rounded up to 16 bytes; each prefetched array holds 2P rows of nx floats.
+__host__ __device__ __forceinline__ int x_rows_offset(int nx, int P) {
+  const int o = nx + spad_size(P * nx);
+  return o + (o & 1);
 }
 
 // ---------------------------------------------------------------- stage I/O
@@ -279,41 +332,17 @@ __device__ __forceinline__ float rl_ratio(float c, float raw, float eps) {
 
 struct RatioStore {
   static constexpr bool kSmem = true;
-  static constexpr bool kGroup = true;
+  static constexpr bool kGroup = false;
   SmemIO io;
-  const float* raw;
-  long long zoff;
+  const float* raw;  // shared: rows y0 .. y0+2P-1 of the slice
   int y0, ny, nx;
   float eps;
-  template <int R>
-  __device__ __forceinline__ void st_group(int v, int base, int stride, const float2* c) const {
+  __device__ __forceinline__ void st(int v, int e, float2 c) const {
     const int ya = y0 + 2 * v;
-    const bool va = ya < ny, vb = ya + 1 < ny;
-    const long long o = zoff + (long long)ya * nx;
-    constexpr int C = R < kStoreBatch ? R : kStoreBatch;
-#pragma unroll
-    for (int q0 = 0; q0 < R; q0 += C) {
-      // the last batch of a radix that is not a multiple of C is partial
-      float ra[C], rb[C];
-#pragma unroll
-      for (int q = 0; q < C; ++q) {
-        ra[q] = 0.f;
-        rb[q] = 0.f;
-        if (q0 + q < R) {
-          const int e = base + (q0 + q) * stride;
-          if (va) ra[q] = __ldg(raw + o + e);
-          if (vb) rb[q] = __ldg(raw + o + nx + e);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < C; ++q) {
-        if (q0 + q < R) {
-          const float2 r = make_float2(va ? rl_ratio(c[q0 + q].x, ra[q], eps) : 0.f,
-                                       vb ? rl_ratio(c[q0 + q].y, rb[q], eps) : 0.f);
-          io.st(v, base + (q0 + q) * stride, r);
-        }
-      }
-    }
+    float2 r = make_float2(0.f, 0.f);
+    if (ya < ny) r.x = rl_ratio(c.x, raw[(2 * v) * nx + e], eps);
+    if (ya + 1 < ny) r.y = rl_ratio(c.y, raw[(2 * v + 1) * nx + e], eps);
+    io.st(v, e, r);
   }
 };
 
@@ -323,71 +352,38 @@ struct RatioStore {
 // (RLgpuImpl.cu:571-633: float products, double sums).
 struct UpdateStore {
   static constexpr bool kSmem = false;
-  static constexpr bool kGroup = true;
-  const float* X;
-  const float* Xm1;
-  float* Xout;
-  float* G;
+  static constexpr bool kGroup = false;
+  const float* Xs;   // shared copies of rows y0 .. y0+2P-1 of X, X_{k-1} and G
+  const float* Xm1s;
+  const float* Gs;
+  float* Xout;       // global
+  float* G;          // global
   float lam;
   int predict, dots;
   long long zoff;
   int y0, ny, nx;
   double* s1;
   double* s2;
-  // The first n of C elements of one row at offsets o + e[q]: all loads
-  // first, then the stores.
-  template <int C>
-  __device__ __forceinline__ void rows(long long o, const int* e, const float* cc, int n) const {
-    float x[C], xm[C], go[C];
-#pragma unroll
-    for (int q = 0; q < C; ++q) {
-      x[q] = 0.f;
-      xm[q] = 0.f;
-      go[q] = 0.f;
-      if (q < n) {
-        x[q] = X[o + e[q]];
-        if (predict) xm[q] = Xm1[o + e[q]];
-        if (dots) go[q] = G[o + e[q]];
-      }
+  __device__ __forceinline__ void one(int rloc, int e, float cc) const {
+    const int l = rloc * nx + e;
+    const float x = Xs[l];
+    const float yv = predict ? predict_y(x, Xm1s[l], lam) : x;
+    float xn = __fmul_rn(cc, yv);
+    xn = xn > 0.f ? xn : 0.f;
+    const float gn = __fsub_rn(xn, yv);
+    if (dots) {
+      const float go = Gs[l];
+      *s1 += (double)__fmul_rn(gn, go);
+      *s2 += (double)__fmul_rn(go, go);
     }
-#pragma unroll
-    for (int q = 0; q < C; ++q) {
-      if (q < n) {
-        const float yv = predict ? predict_y(x[q], xm[q], lam) : x[q];
-        float xn = __fmul_rn(cc[q], yv);
-        xn = xn > 0.f ? xn : 0.f;
-        const float gn = __fsub_rn(xn, yv);
-        if (dots) {
-          *s1 += (double)__fmul_rn(gn, go[q]);
-          *s2 += (double)__fmul_rn(go[q], go[q]);
-        }
-        Xout[o + e[q]] = xn;
-        G[o + e[q]] = gn;
-      }
-    }
+    const long long o = zoff + (long long)(y0 + rloc) * nx + e;
+    Xout[o] = xn;
+    G[o] = gn;
   }
-  template <int R>
-  __device__ __forceinline__ void st_group(int v, int base, int stride, const float2* c) const {
+  __device__ __forceinline__ void st(int v, int e, float2 c) const {
     const int ya = y0 + 2 * v;
-    if (ya >= ny) return;
-    const long long o = zoff + (long long)ya * nx;
-    constexpr int C = R < kStoreBatch ? R : kStoreBatch;
-#pragma unroll
-    for (int q0 = 0; q0 < R; q0 += C) {
-      // the last batch of a radix that is not a multiple of C is partial
-      const int n = (R - q0) < C ? (R - q0) : C;
-      int e[C];
-      float ca[C], cb[C];
-#pragma unroll
-      for (int q = 0; q < C; ++q) {
-        const int qq = (q0 + q < R) ? q0 + q : R - 1;  // clamp the unused lanes
-        e[q] = base + qq * stride;
-        ca[q] = c[qq].x;
-        cb[q] = c[qq].y;
-      }
-      rows<C>(o, e, ca, n);
-      if (ya + 1 < ny) rows<C>(o + nx, e, cb, n);
-    }
+    if (ya < ny) one(2 * v, e, c.x);
+    if (ya + 1 < ny) one(2 * v + 1, e, c.y);
   }
 };
 
@@ -550,10 +546,15 @@ k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __rest
   const SmemIO io{smem + nx, 1, nx};
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
+  float* raws = reinterpret_cast<float*>(smem + x_rows_offset(nx, P));
+  const int nr = min(2 * P, g.ny - y0);
+  prefetch_floats(raws, raw + ((long long)z * g.ny + y0) * nx, nr * nx);
+  cp_async_commit();
   load_twiddles(fx, stw);
   load_packed_spectra(g, S, io, P, z, y0);
+  cp_async_wait_all();
   __syncthreads();
-  const RatioStore rs{io, raw, (long long)z * g.ny * nx, y0, g.ny, nx, eps};
+  const RatioStore rs{io, raws, y0, g.ny, nx, eps};
   fft_run<true>(fx, P, 1.f, false, stw, io, io, rs);
   fft_run<false>(fx, P, 1.f, false, stw, io, io, io);
   store_half_spectra(g, io, P, z, y0, S);
@@ -564,7 +565,7 @@ int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const flo
   const int P = x_pairs(g.nx);
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   int T = threads_for((long long)P * g.nx);
-  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  size_t smem = sizeof(float2) * ((size_t)x_rows_offset(g.nx, P) + (size_t)P * g.nx);
   if (int rc = smem_optin(k_x_inv_ratio_fwd, smem)) return rc;
   k_x_inv_ratio_fwd<<<grid, T, smem, st>>>(g, fx.dev, S, raw, eps, P);
   CDX_LAUNCH_CHECK("k_x_inv_ratio_fwd");
@@ -608,11 +609,23 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* __r
   const SmemIO io{smem + nx, 1, nx};
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
+  // prefetch rows of X, X_{k-1} (when predicting) and G (when the dots are
+  // needed) into shared memory; they are read by the epilogue
+  float* Xs = reinterpret_cast<float*>(smem + x_rows_offset(nx, P));
+  float* Xm1s = Xs + 2 * P * nx;
+  float* Gs = Xm1s + 2 * P * nx;
+  const int nr = min(2 * P, g.ny - y0);
+  const long long roff = ((long long)z * g.ny + y0) * nx;
+  prefetch_floats(Xs, X + roff, nr * nx);
+  if (predict) prefetch_floats(Xm1s, Xm1 + roff, nr * nx);
+  if (dots) prefetch_floats(Gs, G + roff, nr * nx);
+  cp_async_commit();
   load_twiddles(fx, stw);
   load_packed_spectra(g, S, io, P, z, y0);
+  cp_async_wait_all();
   __syncthreads();
   double s1 = 0.0, s2 = 0.0;
-  const UpdateStore us{X, Xm1, Xout, G, predict ? __ldg(lamp) : 0.f, predict, dots,
+  const UpdateStore us{Xs, Xm1s, Gs, Xout, G, predict ? __ldg(lamp) : 0.f, predict, dots,
                        (long long)z * g.ny * nx, y0, g.ny, nx, &s1, &s2};
   fft_run<true>(fx, P, 1.f, false, stw, io, io, us);
   if (!dots) return;
@@ -657,7 +670,7 @@ int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const 
     return cudaErrorInvalidValue;
   }
   int T = threads_for((long long)P * g.nx);
-  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  size_t smem = sizeof(float2) * ((size_t)x_rows_offset(g.nx, P) + 3 * (size_t)P * g.nx);
   if (int rc = smem_optin(k_x_inv_update, smem)) return rc;
   k_x_inv_update<<<grid, T, smem, st>>>(g, fx.dev, S, X, Xm1, lam, predict, Xout, G, dots,
                                         w.partials, w.counter, lam_next, eps, P);

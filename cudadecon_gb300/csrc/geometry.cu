@@ -3,11 +3,11 @@
 // bleach statistics, deskew, rotate, sCMOS camera correction and the
 // texture-filtered affine transform.
 //
-// Where a result must match the reference bit for bit (the deskew and rotate
-// source coordinates, the camcor arithmetic) the arithmetic is written with
-// the same operand types and the same expression shape as the reference
-// kernel, so nvcc evaluates it the same way (double intermediates rounded
-// once to float, the same multiply-add contractions).
+// Where a result must match the reference bit for bit, the arithmetic
+// follows the reference kernel's evaluation exactly: deskew and rotate spell
+// out the roundings and fused multiply-adds with intrinsics (pinned against
+// the reference's compiled kernels), camcor keeps the reference's operand
+// types and expression shape.
 #include "kernels.h"
 
 #include <math.h>
@@ -275,7 +275,10 @@ int mean_above_background(const float* img, long long n, double* d_tmp, unsigned
 // ---------------------------------------------------------------- deskew
 // Shear along x by deskewFactor*(z - nz/2) with linear interpolation inside
 // each x row; padVal outside (reference deskew_kernel, geometryTransform.cu:4-31).
-// The source coordinate is formed in double and rounded once to float.
+// The arithmetic is written out with intrinsics in the order the reference's
+// nvcc build evaluates it (pinned against the reference kernel on the GPU):
+// the source coordinate in double with one fused multiply-add, rounded once
+// to float; the blend (1-offset)*a + offset*b with the first product fused.
 __global__ void k_deskew(const float* __restrict__ in, int nx, int ny, int nz,
                          float* __restrict__ out, int nxOut, int extraShift, double deskewFactor,
                          float padVal) {
@@ -283,12 +286,15 @@ __global__ void k_deskew(const float* __restrict__ in, int nx, int ny, int nz,
   const unsigned yout = blockIdx.y;
   const unsigned zout = blockIdx.z;
   if (xout >= (unsigned)nxOut) return;
-  const float xin = (xout - nxOut / 2. + extraShift) - deskewFactor * (zout - nz / 2.) + nx / 2.;
+  const double a = __dadd_rn(__dsub_rn((double)xout, nxOut / 2.), (double)extraShift);
+  const double b = __dsub_rn((double)zout, nz / 2.);
+  const float xin = __double2float_rn(__dadd_rn(__fma_rn(-deskewFactor, b, a), nx / 2.));
   const size_t indout = ((size_t)zout * ny + yout) * nxOut + xout;
   if (xin >= 0 && xin < nx - 1) {
-    const size_t indin = ((size_t)zout * ny + yout) * nx + (unsigned int)floorf(xin);
-    const float offset = xin - floorf(xin);
-    out[indout] = (1 - offset) * in[indin] + offset * in[indin + 1];
+    const float fl = floorf(xin);
+    const size_t indin = ((size_t)zout * ny + yout) * nx + (unsigned int)fl;
+    const float offset = __fsub_rn(xin, fl);
+    out[indout] = __fmaf_rn(__fsub_rn(1.f, offset), in[indin], __fmul_rn(offset, in[indin + 1]));
   } else {
     out[indout] = padVal;
   }
@@ -310,29 +316,34 @@ struct Rot4 {
   float p[4];
 };
 
+// Arithmetic written out as the reference's nvcc build evaluates it (pinned
+// against the reference kernel on the GPU): each coordinate is
+// fmaf(r0, zc, r1*xc) in float, then the half size is added in double and
+// the sum rounded to float; each of the three blends fuses its first product.
 __global__ void k_rotate(const float* __restrict__ in, int nx_in, int ny, int nz_in,
                          float* __restrict__ out, int nx_out, int nz_out, Rot4 rot) {
   const unsigned xout = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned yout = blockIdx.y;
   const unsigned zout = blockIdx.z;
   if (xout >= (unsigned)nx_out) return;
-  float xout_centered, zout_centered;
-  xout_centered = xout - nx_out / 2.;
-  zout_centered = zout - nz_out / 2.;
-  const float* rotMat = rot.p;
-  const float zin = rotMat[0] * zout_centered + rotMat[1] * xout_centered + nz_in / 2.;
-  const float xin = rotMat[2] * zout_centered + rotMat[3] * xout_centered + nx_in / 2.;
+  const float xc = __double2float_rn(__dsub_rn((double)xout, nx_out / 2.));
+  const float zc = __double2float_rn(__dsub_rn((double)zout, nz_out / 2.));
+  const float zin = __double2float_rn(
+      __dadd_rn((double)__fmaf_rn(rot.p[0], zc, __fmul_rn(rot.p[1], xc)), nz_in / 2.));
+  const float xin = __double2float_rn(
+      __dadd_rn((double)__fmaf_rn(rot.p[2], zc, __fmul_rn(rot.p[3], xc)), nx_in / 2.));
   const size_t nxy_in = (size_t)nx_in * ny;
   const size_t nxy_out = (size_t)nx_out * ny;
   const size_t indout = (size_t)(nz_out - 1 - zout) * nxy_out + (size_t)yout * nx_out + xout;
   if (xin >= 0 && xin < nx_in - 1 && zin >= 0 && zin < nz_in - 1) {
-    const size_t i00 = (size_t)(unsigned)floorf(zin) * nxy_in + (size_t)yout * nx_in +
-                       (unsigned)floorf(xin);
+    const float fz = floorf(zin), fx = floorf(xin);
+    const size_t i00 = (size_t)(unsigned)fz * nxy_in + (size_t)yout * nx_in + (unsigned)fx;
     const size_t i01 = i00 + 1, i10 = i00 + nxy_in, i11 = i10 + 1;
-    const float xoffset = xin - floorf(xin);
-    const float zoffset = zin - floorf(zin);
-    out[indout] = (1 - zoffset) * ((1 - xoffset) * in[i00] + xoffset * in[i01]) +
-                  zoffset * ((1 - xoffset) * in[i10] + xoffset * in[i11]);
+    const float xo = __fsub_rn(xin, fx), zo = __fsub_rn(zin, fz);
+    const float wx = __fsub_rn(1.f, xo), wz = __fsub_rn(1.f, zo);
+    const float a = __fmaf_rn(wx, in[i00], __fmul_rn(xo, in[i01]));
+    const float b = __fmaf_rn(wx, in[i10], __fmul_rn(xo, in[i11]));
+    out[indout] = __fmaf_rn(wz, a, __fmul_rn(zo, b));
   } else {
     out[indout] = 0.f;
   }

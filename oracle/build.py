@@ -1,8 +1,15 @@
 """ORACLE build recipe — test infrastructure only.
 
-Compiles the C restatement geom_oracle.c into oracle/_build/libgeom_oracle.so
-with -ffp-contract=off (so the compiler adds no fused multiply-adds beyond
-the explicit fma() calls; gcc on aarch64 would otherwise contract).
+* geom_oracle.c -> oracle/_build/libgeom_oracle.so, with -ffp-contract=off (so
+  the compiler adds no fused multiply-adds beyond the explicit fma() calls;
+  gcc on aarch64 would otherwise contract).
+* The reference's own CUDA kernels, compiled from its sources where they lie
+  (/root/reference/src/{RLgpuImpl,geometryTransform,camcor}.cu, with its
+  Buffers/ headers) to PTX in oracle/_ref/ — only where the reference is
+  present.  The PTX travels with the repository to the GPU machine, where
+  ref_runner.cu (our launcher, driver API + cuFFT) is compiled against it into
+  oracle/_ref/libref_runner.so.  Nothing here reads the PTX; it is loaded with
+  cuModuleLoad.
 """
 
 from __future__ import annotations
@@ -26,8 +33,54 @@ def build_geom() -> Path:
     return out
 
 
+REF_SRC = Path("/root/reference/src")
+REF_OUT = HERE / "_ref"
+REF_UNITS = ["RLgpuImpl", "geometryTransform", "camcor"]
+
+
+def _nvcc() -> str:
+    p = Path("/usr/local/cuda/bin/nvcc")
+    return str(p) if p.exists() else "nvcc"
+
+
+def build_ref_ptx() -> bool:
+    """Compile the reference's kernels to PTX (only where the reference exists)."""
+    if not (REF_SRC / "RLgpuImpl.cu").exists():
+        return all((REF_OUT / f"{u}.ptx").exists() for u in REF_UNITS)
+    REF_OUT.mkdir(exist_ok=True)
+    for u in REF_UNITS:
+        src, out = REF_SRC / f"{u}.cu", REF_OUT / f"{u}.ptx"
+        if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+            continue
+        cmd = [_nvcc(), "-ptx", "-arch=compute_103a", "-std=c++17", f"-I{REF_SRC}",
+               f"-I{REF_SRC / 'Buffers'}", str(src), "-o", str(out)]
+        subprocess.run(cmd, check=True)
+    return True
+
+
+def build_ref_runner() -> Path | None:
+    """Compile our launcher of the reference kernels (needs the PTX and cuFFT)."""
+    if not all((REF_OUT / f"{u}.ptx").exists() for u in REF_UNITS):
+        return None
+    src, out = HERE / "ref_runner.cu", REF_OUT / "libref_runner.so"
+    if out.exists() and out.stat().st_mtime >= src.stat().st_mtime:
+        return out
+    cmd = [_nvcc(), "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(src), "-o",
+           str(out), "-lcuda", "-lcufft"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print("reference runner not built:", r.stderr[-2000:])
+        return None
+    return out
+
+
 def build_all() -> None:
     build_geom()
+    try:
+        if build_ref_ptx():
+            build_ref_runner()
+    except (subprocess.CalledProcessError, OSError) as e:
+        print("reference kernels not built:", e)
 
 
 if __name__ == "__main__":

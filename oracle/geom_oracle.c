@@ -80,8 +80,9 @@ void oracle_rotate_v(const float* in, int nx_in, int ny, int nz_in, float* out, 
 #undef MAC2
 }
 
-/* The contraction the reference's nvcc build applies (pinned on the GPU). */
-int g_rotate_coord_mode = 2, g_rotate_interp_mode = 1;
+/* The contraction the reference's nvcc build applies to rotate_kernel, as
+ * pinned by tests/golden/golden_rotate.npz (reference kernel output). */
+int g_rotate_coord_mode = 1, g_rotate_interp_mode = 1;
 
 void oracle_rotate(const float* in, int nx_in, int ny, int nz_in, float* out, int nx_out,
                    int nz_out, const float* rot, int contract) {

@@ -449,3 +449,42 @@ def rl_interface(state: InitState, raw_u16, background=100.0, bDoRescale=False,
         if nxr * ny * nzr > rnx * ny * rnz:
             X = X.reshape(-1)[: rnx * ny * rnz].reshape(rnz, ny, rnx)
     return X, desk_out
+
+
+# ---------------------------------------------------------------- affine
+def affine(stack, mat4x4, ra=False, dx=1.0, dy=1.0, dz=1.0):
+    """transformKernel / transformKernelRA (geometryTransform.cu:183-253):
+    trilinear texture fetch with zero border at M*(x, y, z, 1) (+0.5 in the
+    non-RA form; world coordinates with voxel size (dx, dy, dz) in the RA
+    form).  The texture unit's interpolation weights have 8 fractional bits
+    (CUDA Programming Guide, texture fetching); they are rounded to that
+    grid here, which reproduces the hardware to within about 5e-3 of the
+    data range, not bit for bit."""
+    a = np.asarray(stack, dtype=np.float64)
+    nz, ny, nx = a.shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    m = np.asarray(mat4x4, dtype=np.float32).reshape(16)
+    u, v, w = (c.astype(np.float32) for c in (x, y, z))
+    if ra:
+        u, v, w = ((0.5 + (c.astype(np.float64) - 0.5) * float(F32(d))).astype(np.float32)
+                   for c, d in ((u, dx), (v, dy), (w, dz)))
+    t = []
+    for r in range(3):
+        s = (F32(m[4 * r]) * u + F32(m[4 * r + 1]) * v + F32(m[4 * r + 2]) * w + F32(m[4 * r + 3]))
+        t.append((s + F32(0.5)).astype(np.float32) if not ra else s.astype(np.float32))
+    if ra:
+        t = [(0.5 + (c.astype(np.float64) - 0.5) / float(F32(d))).astype(np.float32)
+             for c, d in zip(t, (dx, dy, dz))]
+    xb, yb, zb = (c.astype(np.float64) - 0.5 for c in t)
+    i, j, k = (np.floor(c).astype(np.int64) for c in (xb, yb, zb))
+    ax, ay, az = (np.round((c - f) * 256) / 256 for c, f in ((xb, i), (yb, j), (zb, k)))
+
+    def T(kk, jj, ii):
+        ok = (ii >= 0) & (ii < nx) & (jj >= 0) & (jj < ny) & (kk >= 0) & (kk < nz)
+        return np.where(ok, a[np.clip(kk, 0, nz - 1), np.clip(jj, 0, ny - 1), np.clip(ii, 0, nx - 1)], 0)
+
+    out = ((1 - az) * ((1 - ay) * ((1 - ax) * T(k, j, i) + ax * T(k, j, i + 1)) +
+                       ay * ((1 - ax) * T(k, j + 1, i) + ax * T(k, j + 1, i + 1))) +
+           az * ((1 - ay) * ((1 - ax) * T(k + 1, j, i) + ax * T(k + 1, j, i + 1)) +
+                 ay * ((1 - ax) * T(k + 1, j + 1, i) + ax * T(k + 1, j + 1, i + 1))))
+    return out.astype(np.float32)
