@@ -1,0 +1,51 @@
+// y pass of the 3D transforms: complex FFTs along y of every (kx, z) row.
+#include "decon_common.cuh"
+
+namespace cdx {
+
+// ---------------------------------------------------------------- y pass
+template <bool INV, class Run>
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
+  extern __shared__ float2 smem[];
+  const int ny = g.ny;
+  float2* stw = smem;
+  const SmemIO io{smem + ny, 1, ny};
+  load_twiddles(fy, stw);
+  __syncthreads();
+  const SpecRowIO gio{S, (long long)blockIdx.x * V, (long long)g.nxh * g.nz, g.nyp};
+  Run::template run<INV>(fy, V, 1.f, false, stw, io, gio, gio);
+}
+
+template <bool INV, class Run>
+static int y_go(const Geom& g, const FftDev& f, float2* S, int V, int T, cudaStream_t st) {
+  const long long nrows = (long long)g.nxh * g.nz;
+  size_t smem = fft_smem(g.ny, (long long)V * g.ny);
+  dim3 grid((unsigned)((nrows + V - 1) / V));
+  if (int rc = smem_optin(k_y_pass<INV, Run>, smem)) return rc;
+  k_y_pass<INV, Run><<<grid, T, smem, st>>>(g, f, S, V);
+  CDX_LAUNCH_CHECK("k_y_pass");
+  return 0;
+}
+
+template <bool INV>
+static int y_dispatch(const Geom& g, const FftLen& fy, float2* S, cudaStream_t st) {
+  if (fy.has_static) switch (g.ny) {
+#define CDX_CASE(L, VV) \
+  case L:               \
+    return y_go<INV, StaticRunner<SP##L, VV, false>>(g, fy.sdev, S, VV, splan_threads<SP##L, VV>(), st);
+      CDX_Y_PLANS(CDX_CASE)
+#undef CDX_CASE
+      default:
+        break;
+    }
+  int V = 2048 / g.ny;
+  if (V < 1) V = 1;
+  return y_go<INV, GenericRunner>(g, fy.dev, S, V, threads_for((long long)V * g.ny), st);
+}
+
+int launch_y_pass(const Geom& g, const FftLen& fy, float2* S, bool inverse, cudaStream_t st) {
+  return inverse ? y_dispatch<true>(g, fy, S, st) : y_dispatch<false>(g, fy, S, st);
+}
+
+}  // namespace cdx

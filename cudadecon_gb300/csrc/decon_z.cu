@@ -1,0 +1,97 @@
+// z pass: forward FFT along z, OTF multiply (interpolated on the fly),
+// inverse FFT along z.
+#include "decon_common.cuh"
+
+namespace cdx {
+
+// ---------------------------------------------------------------- z pass
+// Columns (consecutive y) per z tile: 16 (128-byte runs) while the tile fits
+// kMaxThreads * kEpt elements, fewer for long z.
+static int z_cols(int nz) {
+  int w = (kMaxThreads * kEpt) / nz;
+  if (w > 16) w = 16;
+  if (w < 1) w = 1;
+  return w;
+}
+
+template <class Run>
+__global__ void __launch_bounds__(kMaxThreads, 1)
+k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int W) {
+  extern __shared__ float2 smem[];
+  const int nz = g.nz;
+  const int kx = blockIdx.y;
+  const int y0 = blockIdx.x * W;
+  float2* stw = smem;
+  const SmemIO io{smem + nz, W, 1};
+  float2* otf_tile = smem + nz + spad_size(W * nz);
+  load_twiddles(fz, stw);
+  const float invW = 1.f / (float)W;
+  const SpecColIO gio{S + (long long)kx * g.plane, y0, g.ny, g.nyp};
+  if (fwd_only) {
+    __syncthreads();
+    Run::template run<false>(fz, W, invW, true, stw, io, gio, gio);
+    return;
+  }
+  // OTF of every (y, z) of the tile, interpolated on the fly from the
+  // kz-resampled radial table (dev_otfinterpolate RA branch,
+  // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
+  // read from the precomputed 3D array
+  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+    const int w = idx % W;
+    const int z = idx / W;
+    const int y = y0 + w;
+    float2 o = make_float2(0.f, 0.f);
+    if (y < g.ny) {
+      if (otf.mode == 1) {
+        o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
+      } else {
+        const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+        const float fx = (float)kx * otf.kxscale;
+        const float fy = (float)ky * otf.kyscale;
+        const float kr = sqrtf(fx * fx + fy * fy);
+        if (kr < (float)(otf.nr - 1)) {
+          const int ir = (int)floorf(kr);
+          const float ar = kr - (float)ir;
+          const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
+          const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
+          o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+        }
+      }
+    }
+    otf_tile[idx] = o;
+  }
+  __syncthreads();
+  const OtfMulStore ost{io, otf_tile, W, conj};
+  Run::template run<false>(fz, W, invW, true, stw, io, gio, ost);
+  Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
+}
+
+template <class Run>
+static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bool conj,
+                bool fwd_only, int W, int T, cudaStream_t st) {
+  dim3 grid(ceil_div(g.ny, W), g.nxh);
+  size_t smem = fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
+  if (int rc = smem_optin(k_z_pass<Run>, smem)) return rc;
+  k_z_pass<Run><<<grid, T, smem, st>>>(g, f, S, otf, conj ? 1 : 0, fwd_only ? 1 : 0, W);
+  CDX_LAUNCH_CHECK("k_z_pass");
+  return 0;
+}
+
+int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf, bool conj,
+                  cudaStream_t st, bool fwd_only) {
+  if (fz.has_static) switch (g.nz) {
+#define CDX_CASE(L, WW)                                                                        \
+  case L:                                                                                      \
+    return z_go<StaticRunner<SP##L, WW, true>>(g, fz.sdev, S, otf, conj, fwd_only, WW,       \
+                                               splan_threads<SP##L, WW>(), st);
+      CDX_Z_PLANS(CDX_CASE)
+#undef CDX_CASE
+      default:
+        break;
+    }
+  const int W = z_cols(g.nz);
+  return z_go<GenericRunner>(g, fz.dev, S, otf, conj, fwd_only, W,
+                             threads_for((long long)W * g.nz), st);
+}
+
+}  // namespace cdx

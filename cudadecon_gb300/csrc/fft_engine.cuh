@@ -38,18 +38,18 @@ constexpr int kMaxFftLen = kMaxThreads * kEpt;
 // ------------------------------------------------------------- constants
 // cos(2*pi*m/R) and sin(2*pi*m/R) for the odd radices, m = 0..R-1.
 template <int R>
-__device__ __forceinline__ float odd_cos(int m);
+__host__ __device__ __forceinline__ float odd_cos(int m);
 template <int R>
-__device__ __forceinline__ float odd_sin(int m);
+__host__ __device__ __forceinline__ float odd_sin(int m);
 
 template <>
-__device__ __forceinline__ float odd_cos<3>(int m) { return m == 0 ? 1.f : -0.5f; }
+__host__ __device__ __forceinline__ float odd_cos<3>(int m) { return m == 0 ? 1.f : -0.5f; }
 template <>
-__device__ __forceinline__ float odd_sin<3>(int m) {
+__host__ __device__ __forceinline__ float odd_sin<3>(int m) {
   return m == 0 ? 0.f : (m == 1 ? 8.660254038e-01f : -8.660254038e-01f);
 }
 template <>
-__device__ __forceinline__ float odd_cos<5>(int m) {
+__host__ __device__ __forceinline__ float odd_cos<5>(int m) {
   switch (m) {
     case 0: return 1.f;
     case 1: case 4: return 3.090169944e-01f;
@@ -57,7 +57,7 @@ __device__ __forceinline__ float odd_cos<5>(int m) {
   }
 }
 template <>
-__device__ __forceinline__ float odd_sin<5>(int m) {
+__host__ __device__ __forceinline__ float odd_sin<5>(int m) {
   switch (m) {
     case 0: return 0.f;
     case 1: return 9.510565163e-01f;
@@ -67,7 +67,7 @@ __device__ __forceinline__ float odd_sin<5>(int m) {
   }
 }
 template <>
-__device__ __forceinline__ float odd_cos<7>(int m) {
+__host__ __device__ __forceinline__ float odd_cos<7>(int m) {
   switch (m) {
     case 0: return 1.f;
     case 1: case 6: return 6.234898019e-01f;
@@ -76,7 +76,7 @@ __device__ __forceinline__ float odd_cos<7>(int m) {
   }
 }
 template <>
-__device__ __forceinline__ float odd_sin<7>(int m) {
+__host__ __device__ __forceinline__ float odd_sin<7>(int m) {
   switch (m) {
     case 0: return 0.f;
     case 1: return 7.818314825e-01f;
@@ -88,7 +88,7 @@ __device__ __forceinline__ float odd_sin<7>(int m) {
   }
 }
 template <>
-__device__ __forceinline__ float odd_cos<9>(int m) {
+__host__ __device__ __forceinline__ float odd_cos<9>(int m) {
   switch (m) {
     case 0: return 1.f;
     case 1: case 8: return 7.660444431e-01f;
@@ -98,7 +98,7 @@ __device__ __forceinline__ float odd_cos<9>(int m) {
   }
 }
 template <>
-__device__ __forceinline__ float odd_sin<9>(int m) {
+__host__ __device__ __forceinline__ float odd_sin<9>(int m) {
   switch (m) {
     case 0: return 0.f;
     case 1: return 6.427876097e-01f;
@@ -121,7 +121,7 @@ struct Dft;
 
 template <bool INV>
 struct Dft<2, INV> {
-  __device__ __forceinline__ static void run(float2* x) {
+  __host__ __device__ __forceinline__ static void run(float2* x) {
     float2 a = x[0], b = x[1];
     x[0] = cadd(a, b);
     x[1] = csub(a, b);
@@ -130,11 +130,11 @@ struct Dft<2, INV> {
 
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
-__device__ __forceinline__ float2 rot_q(float2 a) { return INV ? mul_pi(a) : mul_mi(a); }
+__host__ __device__ __forceinline__ float2 rot_q(float2 a) { return INV ? mul_pi(a) : mul_mi(a); }
 
 template <bool INV>
 struct Dft<4, INV> {
-  __device__ __forceinline__ static void run(float2* x) {
+  __host__ __device__ __forceinline__ static void run(float2* x) {
     float2 a = cadd(x[0], x[2]), b = csub(x[0], x[2]);
     float2 c = cadd(x[1], x[3]), d = rot_q<INV>(csub(x[1], x[3]));
     x[0] = cadd(a, c);
@@ -147,7 +147,7 @@ struct Dft<4, INV> {
 template <bool INV>
 struct Dft<8, INV> {
   // one radix-2 decimation-in-frequency step followed by two radix-4 DFTs
-  __device__ __forceinline__ static void run(float2* x) {
+  __host__ __device__ __forceinline__ static void run(float2* x) {
     const float h = 7.071067812e-01f;
     float2 u[4], v[4];
 #pragma unroll
@@ -174,7 +174,7 @@ struct Dft<8, INV> {
 template <bool INV>
 struct Dft<16, INV> {
   // 4 x 4 decomposition: n = n1 + 4*n2, k = 4*k1 + k2.
-  __device__ __forceinline__ static void run(float2* x) {
+  __host__ __device__ __forceinline__ static void run(float2* x) {
     const float c1 = 9.238795325e-01f, s1 = 3.826834324e-01f, h = 7.071067812e-01f;
     float2 t[4][4];
 #pragma unroll
@@ -217,7 +217,7 @@ struct Dft<16, INV> {
 // Odd radix by the symmetric/antisymmetric pairing of inputs p and R-p.
 template <int R, bool INV>
 struct DftOdd {
-  __device__ __forceinline__ static void run(float2* x) {
+  __host__ __device__ __forceinline__ static void run(float2* x) {
     constexpr int H = (R - 1) / 2;
     float2 s[H + 1], d[H + 1];
 #pragma unroll

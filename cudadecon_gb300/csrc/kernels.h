@@ -40,9 +40,14 @@ struct RawOtfDims {
 };
 
 // FFT plan for one length (host side owns the twiddle table).
+// When the length is in the registry of specialised plans (static_plans.cuh),
+// sdev holds that plan (its radices and twiddle table) as well.
 struct FftLen {
   FftDev dev;
   float2* d_tw = nullptr;
+  bool has_static = false;
+  FftDev sdev;
+  float2* d_tws = nullptr;
 };
 int fft_len_init(FftLen& f, int L);
 void fft_len_free(FftLen& f);

@@ -1,0 +1,49 @@
+// Registry of the compile-time specialised transform lengths.
+//
+// CDX_SPLAN_LIST gives each registered length and its radices (their
+// product is the length; radices up to 32 points run in registers).  The
+// per-axis lists say for which pass kernels a length is instantiated and
+// with which tile: x passes with P row pairs per block (the same P as the
+// generic x tiles), y passes with V rows, z passes with W columns.  Other
+// lengths use the generic engine.
+#pragma once
+
+#include <vector>
+
+#include "fft_static.cuh"
+
+#define CDX_SPLAN_LIST(F) \
+  F(32, 8, 4)             \
+  F(64, 8, 8)             \
+  F(100, 10, 10)          \
+  F(128, 16, 8)           \
+  F(256, 16, 16)          \
+  F(512, 32, 16)          \
+  F(756, 28, 27)          \
+  F(1024, 32, 32)
+
+#define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 4) F(1024, 4)
+#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 2)
+#define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
+
+namespace cdx {
+
+#define CDX_DEF_SPLAN(L, ...) using SP##L = SPlan<L, __VA_ARGS__>;
+CDX_SPLAN_LIST(CDX_DEF_SPLAN)
+#undef CDX_DEF_SPLAN
+
+// Radices of the registered plan for length L (false when L is not registered).
+inline bool static_radices(int L, std::vector<int>& rad) {
+  switch (L) {
+#define CDX_RAD_CASE(LL, ...) \
+  case LL:                    \
+    rad = {__VA_ARGS__};      \
+    return true;
+    CDX_SPLAN_LIST(CDX_RAD_CASE)
+#undef CDX_RAD_CASE
+    default:
+      return false;
+  }
+}
+
+}  // namespace cdx

@@ -51,7 +51,10 @@ def _oracle_state(oracle, shape_zyx, table, **kw):
 # ---------------------------------------------------------------- FFT
 @pytest.mark.parametrize("shape", [(4, 6, 10), (9, 15, 21), (16, 18, 20), (25, 27, 49),
                                    (7, 5, 3), (32, 64, 100), (64, 256, 256), (100, 256, 756),
-                                   (27, 35, 1620)])
+                                   (27, 35, 1620),
+                                   # every length of the specialised-plan registry on each axis
+                                   (128, 128, 128), (32, 512, 1024), (64, 1024, 256),
+                                   (256, 64, 512), (100, 18, 756)])
 def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
     torch = torch_cuda
     nz, ny, nx = shape
@@ -65,7 +68,8 @@ def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
     assert rel_l2(out.cpu().numpy(), ref) < 2e-6
 
 
-@pytest.mark.parametrize("shape", [(16, 32, 30), (20, 24, 45), (64, 256, 256)])
+@pytest.mark.parametrize("shape", [(16, 32, 30), (20, 24, 45), (64, 256, 256), (100, 256, 756),
+                                   (128, 128, 128), (32, 512, 1024)])
 @pytest.mark.parametrize("conj", [0, 1])
 def test_conv3d_matches_oracle(cdx, oracle, torch_cuda, tmp_path, shape, conj):
     torch = torch_cuda
