@@ -331,8 +331,11 @@ static int rl_iterations(Session& s, int nIter, float** final_x) {
     mark();
     if ((rc = launch_y_pass(g, p.fy, s.S.p, true, s.stream))) return rc;
     mark();
-    if ((rc = launch_x_inv_update(g, p.fx, s.S.p, X, Xm1, lam_k, predict, Xm1, s.G.p, k >= 1, w,
-                                  lam_n, eps, s.stream)))
+    // x_fwd wrote the prediction Y over Xm1 when predicting (else Y = X);
+    // the new estimate replaces it in place
+    const float* Y = predict ? Xm1 : X;
+    if ((rc = launch_x_inv_update(g, p.fx, s.S.p, Y, Xm1, s.G.p, k >= 1, w, lam_n, eps,
+                                  s.stream)))
       return rc;
     mark();
     if (prof && g_prof.used >= 10 * 64) prof_collect();

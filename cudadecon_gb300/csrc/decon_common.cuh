@@ -1,7 +1,7 @@
-// Device helpers and tile I/O shared by the pass kernels (decon_x_fwd.cu,
-// decon_x_inv.cu, decon_yz.cu): packed-row spectrum split/merge, async row
-// copies into shared memory, and the first-stage loaders / last-stage
-// storers that fuse the RL prologue and epilogues into the transforms.
+// Device helpers and tile I/O shared by the pass kernels (decon_x_*.cu,
+// decon_y.cu, decon_z.cu): packed-row spectrum split/merge, async copies
+// into shared memory, and the first-stage loaders / last-stage storers that
+// fuse the RL prologue and epilogues into the transforms.
 #pragma once
 
 #include "kernels.h"
@@ -72,59 +72,22 @@ static int smem_optin(K kernel, size_t bytes) {
   return 0;
 }
 
-// Store the packed-row FFT held in the tile (P vectors of length nx) into S.
-__device__ __forceinline__ void store_half_spectra(const Geom& g, const SmemIO& io, int P, int z,
+// Store the packed-row FFT held in the tile (P vectors of length nx) into S
+// (PC: P as a compile-time constant, 0 when it is only known at run time).
+template <int PC, class IO>
+__device__ __forceinline__ void store_half_spectra(const Geom& g, const IO& io, int P, int z,
                                                    int y0, float2* S) {
   const int nx = g.nx;
+  const float invP = 1.f / (float)P;
   for (int idx = threadIdx.x; idx < g.nxh * P; idx += blockDim.x) {
-    const int p = idx % P;
-    const int k = idx / P;
+    int p, k;
+    divmod_small<PC>(idx, P, invP, k, p);
     const int ya = y0 + 2 * p;
     if (ya >= g.ny) continue;
     const float2 zk = io.ld(p, k);
     const float2 zm = io.ld(p, k == 0 ? 0 : nx - k);
     *reinterpret_cast<float4*>(S + (long long)k * g.plane + (long long)z * g.nyp + ya) =
         split_pair(zk, zm);
-  }
-}
-
-// Load the two half spectra of rows (ya, ya+1) and rebuild the packed
-// full-length spectrum Z = A + iB in the tile.  The imaginary parts of the
-// DC and (even nx) Nyquist bins are dropped, as a C2R transform does.
-__device__ __forceinline__ void load_packed_spectra(const Geom& g, const float2* S, const SmemIO& io,
-                                                    int P, int z, int y0) {
-  const int nx = g.nx;
-  const int n = g.nxh * P;
-  const int T = blockDim.x;
-  constexpr int B = 8;  // loads issued before the first shared store
-  for (int base = threadIdx.x; base < n; base += B * T) {
-    float4 v[B];
-#pragma unroll
-    for (int b = 0; b < B; ++b) {
-      const int idx = base + b * T;
-      const int p = idx % P;
-      const int k = idx / P;
-      const int ya = y0 + 2 * p;
-      v[b] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (idx < n && ya < g.ny)
-        v[b] = __ldg(reinterpret_cast<const float4*>(S + (long long)k * g.plane +
-                                                     (long long)z * g.nyp + ya));
-    }
-#pragma unroll
-    for (int b = 0; b < B; ++b) {
-      const int idx = base + b * T;
-      if (idx >= n) break;
-      const int p = idx % P;
-      const int k = idx / P;
-      float4 w = v[b];
-      if (k == 0 || 2 * k == nx) {
-        w.y = 0.f;
-        w.w = 0.f;
-      }
-      // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
-      io.st(p, k, make_float2(w.x - w.w, w.y + w.z));
-      if (k > 0 && 2 * k != nx) io.st(p, nx - k, make_float2(w.x + w.w, w.z - w.y));
-    }
   }
 }
 
@@ -157,11 +120,38 @@ __device__ __forceinline__ void prefetch_floats(float* dst, const float* src, in
   }
 }
 
-// Shared float2 offset after the twiddles and the padded tile of an x kernel,
-// rounded up to 16 bytes; each prefetched array holds 2P rows of nx floats.
+// Shared-memory layout of an x kernel, in float2 units: the twiddles (nx),
+// then the tile region (16-byte aligned), then the prefetched row arrays
+// (2P rows of nx floats each).  The tile region holds the padded transform
+// tile and, before the first stage, the staged half spectra (P vectors of
+// nx/2+1 float4) that the first stage reads: the two alias.
+__host__ __device__ __forceinline__ int x_tile_offset(int nx) { return nx + (nx & 1); }
+__host__ __device__ __forceinline__ int x_tile_size(int nx, int P) {
+  const int a = spad_size(P * nx);
+  const int b = 2 * (nx / 2 + 1) * P;
+  const int m = a > b ? a : b;
+  return m + (m & 1);
+}
 __host__ __device__ __forceinline__ int x_rows_offset(int nx, int P) {
-  const int o = nx + spad_size(P * nx);
-  return o + (o & 1);
+  return x_tile_offset(nx) + x_tile_size(nx, P);
+}
+
+// Issue cp.async copies of the half spectra of rows (y0+2p, y0+2p+1),
+// p < P, of slice z into the staging array stg[p * nxh + k] (float4 =
+// A[k], B[k]); pairs beyond ny are not copied.  Consecutive threads copy
+// the P pairs of one kx (a contiguous run of 16P bytes in S).
+template <int PC>
+__device__ __forceinline__ void prefetch_packed_spectra(const Geom& g, const float2* S, float4* stg,
+                                                        int P, int z, int y0) {
+  const int nxh = g.nxh;
+  const int n = nxh * P;
+  const float invP = 1.f / (float)P;
+  const long long zo = (long long)z * g.nyp + y0;
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    int p, k;
+    divmod_small<PC>(idx, P, invP, k, p);
+    if (y0 + 2 * p < g.ny) cp_async16(stg + p * nxh + k, S + (long long)k * g.plane + zo + 2 * p);
+  }
 }
 
 // ---------------------------------------------------------------- stage I/O
@@ -193,6 +183,54 @@ struct RowPairLoad {
       }
     }
     return make_float2(a, b);
+  }
+};
+
+// First-stage loader of the forward x pass from rows prefetched into shared
+// memory (Xs, Xm1s: 2P rows of nx floats, nr of them valid).
+struct RowPairSmemLoad {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  const float* Xs;
+  const float* Xm1s;
+  float lam;
+  int predict, nr, nx;
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    const int ra = 2 * v;
+    float a = 0.f, b = 0.f;
+    if (ra < nr) {
+      const int o = ra * nx + e;
+      a = Xs[o];
+      if (predict) a = predict_y(a, Xm1s[o], lam);
+      if (ra + 1 < nr) {
+        b = Xs[o + nx];
+        if (predict) b = predict_y(b, Xm1s[o + nx], lam);
+      }
+    }
+    return make_float2(a, b);
+  }
+};
+
+// First-stage loader of the inverse x passes: element e of the packed
+// full-length spectrum Z = A + iB of pair v, rebuilt from the staged half
+// spectra (prefetch_packed_spectra).  The imaginary parts of the DC and
+// (even nx) Nyquist bins are dropped, as a C2R transform does.
+struct PackedSpecLoad {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  const float4* stg;
+  int nxh, nx, npairs;  // npairs: pairs with rows inside the volume
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    if (v >= npairs) return make_float2(0.f, 0.f);
+    const bool lo = e < nxh;
+    const int k = lo ? e : nx - e;
+    float4 w = stg[v * nxh + k];
+    if (k == 0 || 2 * k == nx) {
+      w.y = 0.f;
+      w.w = 0.f;
+    }
+    // Z[k] = A + iB; Z[nx-k] = conj(A) + i conj(B)
+    return lo ? make_float2(w.x - w.w, w.y + w.z) : make_float2(w.x + w.w, w.z - w.y);
   }
 };
 
@@ -247,16 +285,21 @@ struct OtfMulStore {
 // written to the tile for the forward transform that follows.
 __device__ __forceinline__ float rl_ratio(float c, float raw, float eps) {
   float v = fabsf(c) > 0.f ? c : eps;
-  v = __fadd_rn(__fdiv_rn(raw, v), eps);
+  // 0 / v is a signed zero and the sum with eps is eps either way; zero
+  // numerators (common after background subtraction) skip the division,
+  // whose general path is far slower for them.
+  const float q = __fdiv_rn(raw == 0.f ? 1.f : raw, v);
+  v = __fadd_rn(raw == 0.f ? 0.f : q, eps);
   v = v > 10.f ? 10.f : v;
   v = v < -10.f ? -10.f : v;
   return v;
 }
 
+template <class IO>
 struct RatioStore {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
-  SmemIO io;
+  IO io;
   const float* raw;  // shared: rows y0 .. y0+2P-1 of the slice
   int y0, ny, nx;
   float eps;
@@ -266,46 +309,6 @@ struct RatioStore {
     if (ya < ny) r.x = rl_ratio(c.x, raw[(2 * v) * nx + e], eps);
     if (ya + 1 < ny) r.y = rl_ratio(c.y, raw[(2 * v + 1) * nx + e], eps);
     io.st(v, e, r);
-  }
-};
-
-// Last inverse x stage of the second convolution: estimate update
-// (currEstimate_kernel + currPrevDiff_kernel, RLgpuImpl.cu:462-470, 501-508)
-// with the Biggs-Andrews dot products of innerProduct_kernel
-// (RLgpuImpl.cu:571-633: float products, double sums).
-struct UpdateStore {
-  static constexpr bool kSmem = false;
-  static constexpr bool kGroup = false;
-  const float* Xs;   // shared copies of rows y0 .. y0+2P-1 of X, X_{k-1} and G
-  const float* Xm1s;
-  const float* Gs;
-  float* Xout;       // global
-  float* G;          // global
-  float lam;
-  int predict, dots;
-  long long zoff;
-  int y0, ny, nx;
-  float* acc;  // float-float accumulators: s1 (hi, lo), s2 (hi, lo)
-  __device__ __forceinline__ void one(int rloc, int e, float cc) const {
-    const int l = rloc * nx + e;
-    const float x = Xs[l];
-    const float yv = predict ? predict_y(x, Xm1s[l], lam) : x;
-    float xn = __fmul_rn(cc, yv);
-    xn = xn > 0.f ? xn : 0.f;
-    const float gn = __fsub_rn(xn, yv);
-    if (dots) {
-      const float go = Gs[l];
-      acc_add(acc[0], acc[1], __fmul_rn(gn, go));
-      acc_add(acc[2], acc[3], __fmul_rn(go, go));
-    }
-    const long long o = zoff + (long long)(y0 + rloc) * nx + e;
-    Xout[o] = xn;
-    G[o] = gn;
-  }
-  __device__ __forceinline__ void st(int v, int e, float2 c) const {
-    const int ya = y0 + 2 * v;
-    if (ya < ny) one(2 * v, e, c.x);
-    if (ya + 1 < ny) one(2 * v + 1, e, c.y);
   }
 };
 

@@ -1,5 +1,7 @@
 // Forward x pass of the RL iteration (prediction prologue + R2C along x) and
 // the plain inverse x pass used by the convolution test hook.
+#include <algorithm>
+
 #include "decon_common.cuh"
 
 namespace cdx {
@@ -7,34 +9,79 @@ namespace cdx {
 // ---------------------------------------------------------------- x forward
 template <class Run>
 __global__ void __launch_bounds__(kMaxThreads, 1)
-k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, const float* __restrict__ Xm1,
-        const float* __restrict__ lamp, int predict, float2* __restrict__ S, int P) {
-  extern __shared__ float2 smem[];
+k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, float* Xm1, const float* __restrict__ lamp,
+        int predict, float2* __restrict__ S, int Pa) {
+  const int P = tile_vectors<Run>(Pa);
+  extern __shared__ __align__(16) float2 smem[];
   const int nx = g.nx;
   float2* stw = smem;
-  const SmemIO io{smem + nx, 1, nx};
+  const auto io = Run::row_tile(smem + x_tile_offset(nx), nx);
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
+  // The rows of X (and X_{k-1}) are copied into the tile region with
+  // cp.async; the first stage reads them from there before it writes the
+  // tile (the two alias).
+  float* Xs = reinterpret_cast<float*>(io.sm);
+  float* Xm1s = Xs + 2 * P * nx;
+  const int nr = min(2 * P, g.ny - y0);
+  const long long roff = ((long long)z * g.ny + y0) * nx;
+  prefetch_floats(Xs, X + roff, nr * nx);
+  if (predict) prefetch_floats(Xm1s, Xm1 + roff, nr * nx);
+  cp_async_commit();
+  const float lam = predict ? __ldg(lamp) : 0.f;
   load_twiddles(fx, stw);
+  cp_async_wait_all();
   __syncthreads();
-  const RowPairLoad ld{X, Xm1, predict ? __ldg(lamp) : 0.f, predict, (long long)z * g.ny * nx,
-                       y0, g.ny, nx};
+  if (predict) {
+    // prediction of updatePrediction_kernel (RLgpuImpl.cu:658-666), kept in
+    // Xs for the transform and written over the block's rows of X_{k-1}
+    float* Yg = Xm1 + roff;
+    const int n = nr * nx;
+    if (((reinterpret_cast<unsigned long long>(Yg) | reinterpret_cast<unsigned long long>(Xm1s)) &
+         15) == 0) {
+      const int n4 = n >> 2;
+      float4* xs4 = reinterpret_cast<float4*>(Xs);
+      const float4* ms4 = reinterpret_cast<const float4*>(Xm1s);
+      float4* yg4 = reinterpret_cast<float4*>(Yg);
+      for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+        const float4 a = xs4[i], m = ms4[i];
+        const float4 y = make_float4(predict_y(a.x, m.x, lam), predict_y(a.y, m.y, lam),
+                                     predict_y(a.z, m.z, lam), predict_y(a.w, m.w, lam));
+        xs4[i] = y;
+        yg4[i] = y;
+      }
+      for (int i = 4 * n4 + threadIdx.x; i < n; i += blockDim.x) {
+        const float y = predict_y(Xs[i], Xm1s[i], lam);
+        Xs[i] = y;
+        Yg[i] = y;
+      }
+    } else {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float y = predict_y(Xs[i], Xm1s[i], lam);
+        Xs[i] = y;
+        Yg[i] = y;
+      }
+    }
+    __syncthreads();
+  }
+  const RowPairSmemLoad ld{Xs, nullptr, 0.f, 0, nr, nx};
   Run::template run<false>(fx, P, 1.f, false, stw, io, ld, io);
-  store_half_spectra(g, io, P, z, y0, S);
+  store_half_spectra<Run::kV>(g, io, P, z, y0, S);
 }
 
 template <class Run>
-static int x_fwd_go(const Geom& g, const FftDev& f, const float* X, const float* Xm1,
+static int x_fwd_go(const Geom& g, const FftDev& f, const float* X, float* Xm1,
                     const float* lam, int predict, float2* S, int P, int T, cudaStream_t st) {
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
-  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  const int region = std::max(x_tile_size(g.nx, P), 2 * P * g.nx);
+  size_t smem = sizeof(float2) * ((size_t)x_tile_offset(g.nx) + (size_t)region);
   if (int rc = smem_optin(k_x_fwd<Run>, smem)) return rc;
   k_x_fwd<Run><<<grid, T, smem, st>>>(g, f, X, Xm1, lam, predict, S, P);
   CDX_LAUNCH_CHECK("k_x_fwd");
   return 0;
 }
 
-int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* Xm1,
+int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, float* Xm1,
                  const float* lam, int predict, float2* S, cudaStream_t st) {
   if (fx.has_static) switch (g.nx) {
 #define CDX_CASE(L, PP)                                                                      \
@@ -54,25 +101,30 @@ int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* X
 
 template <class Run>
 __global__ void __launch_bounds__(kMaxThreads, 1)
-k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S, float* __restrict__ out, int P) {
-  extern __shared__ float2 smem[];
+k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S, float* __restrict__ out, int Pa) {
+  const int P = tile_vectors<Run>(Pa);
+  extern __shared__ __align__(16) float2 smem[];
   const int nx = g.nx;
   float2* stw = smem;
-  const SmemIO io{smem + nx, 1, nx};
+  const auto io = Run::row_tile(smem + x_tile_offset(nx), nx);
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
+  float4* stg = reinterpret_cast<float4*>(io.sm);
+  prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
+  cp_async_commit();
   load_twiddles(fx, stw);
-  load_packed_spectra(g, S, io, P, z, y0);
+  cp_async_wait_all();
   __syncthreads();
+  const PackedSpecLoad ld{stg, g.nxh, nx, min(P, (g.ny - y0 + 1) / 2)};
   const PlainRowStore ps{out, (long long)z * g.ny * nx, y0, g.ny, nx};
-  Run::template run<true>(fx, P, 1.f, false, stw, io, io, ps);
+  Run::template run<true>(fx, P, 1.f, false, stw, io, ld, ps);
 }
 
 template <class Run>
 static int x_plain_go(const Geom& g, const FftDev& f, const float2* S, float* out, int P, int T,
                       cudaStream_t st) {
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
-  size_t smem = fft_smem(g.nx, (long long)P * g.nx);
+  size_t smem = sizeof(float2) * (size_t)x_rows_offset(g.nx, P);
   if (int rc = smem_optin(k_x_inv_plain<Run>, smem)) return rc;
   k_x_inv_plain<Run><<<grid, T, smem, st>>>(g, f, S, out, P);
   CDX_LAUNCH_CHECK("k_x_inv_plain");

@@ -8,25 +8,30 @@ namespace cdx {
 template <class Run>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __restrict__ raw,
-                  float eps, int P) {
-  extern __shared__ float2 smem[];
+                  float eps, int Pa) {
+  const int P = tile_vectors<Run>(Pa);
+  extern __shared__ __align__(16) float2 smem[];
   const int nx = g.nx;
   float2* stw = smem;
-  const SmemIO io{smem + nx, 1, nx};
+  const auto io = Run::row_tile(smem + x_tile_offset(nx), nx);
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
+  // Half spectra (staged in the tile region) and raw rows are copied with
+  // cp.async; the first stage rebuilds the packed spectra from the stage.
+  float4* stg = reinterpret_cast<float4*>(io.sm);
   float* raws = reinterpret_cast<float*>(smem + x_rows_offset(nx, P));
   const int nr = min(2 * P, g.ny - y0);
+  prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
   prefetch_floats(raws, raw + ((long long)z * g.ny + y0) * nx, nr * nx);
   cp_async_commit();
   load_twiddles(fx, stw);
-  load_packed_spectra(g, S, io, P, z, y0);
   cp_async_wait_all();
   __syncthreads();
-  const RatioStore rs{io, raws, y0, g.ny, nx, eps};
-  Run::template run<true>(fx, P, 1.f, false, stw, io, io, rs);
+  const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
+  const RatioStore<typename Run::Tile> rs{io, raws, y0, g.ny, nx, eps};
+  Run::template run<true>(fx, P, 1.f, false, stw, io, ld, rs);
   Run::template run<false>(fx, P, 1.f, false, stw, io, io, io);
-  store_half_spectra(g, io, P, z, y0, S);
+  store_half_spectra<Run::kV>(g, io, P, z, y0, S);
 }
 
 template <class Run>

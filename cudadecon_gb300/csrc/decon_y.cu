@@ -10,7 +10,7 @@ k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
   extern __shared__ float2 smem[];
   const int ny = g.ny;
   float2* stw = smem;
-  const SmemIO io{smem + ny, 1, ny};
+  const auto io = Run::row_tile(smem + ny, ny);
   load_twiddles(fy, stw);
   __syncthreads();
   const SpecRowIO gio{S, (long long)blockIdx.x * V, (long long)g.nxh * g.nz, g.nyp};

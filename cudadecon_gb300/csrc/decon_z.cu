@@ -16,7 +16,8 @@ static int z_cols(int nz) {
 
 template <class Run>
 __global__ void __launch_bounds__(kMaxThreads, 1)
-k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int W) {
+k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int Wa) {
+  const int W = tile_vectors<Run>(Wa);
   extern __shared__ float2 smem[];
   const int nz = g.nz;
   const int kx = blockIdx.y;
@@ -37,8 +38,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
   // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
   // read from the precomputed 3D array
   for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-    const int w = idx % W;
-    const int z = idx / W;
+    int w, z;
+    divmod_small<Run::kV>(idx, W, invW, z, w);
     const int y = y0 + w;
     float2 o = make_float2(0.f, 0.f);
     if (y < g.ny) {

@@ -85,15 +85,94 @@ __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St
   if (SYNC_END) __syncthreads();
 }
 
+// Unpadded tile in natural order: element e of vector v at sm[v * vs + e].
+// The static transforms read and write natural-order tiles at unit stride
+// across threads (element j + r*LR of butterfly j), so they need no padding.
+struct NatIO {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  float2* sm;
+  int vs;
+  __device__ __forceinline__ float2 ld(int v, int e) const { return sm[v * vs + e]; }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[v * vs + e] = x; }
+};
+
+// Float2s of the middle layout of a two-radix plan over V vectors.
+template <class Plan, int V>
+constexpr int splan_mid_size() {
+  return V * Plan::q(1) * (Plan::q(0) + 1);
+}
+
+// Two-radix transform L = Q0*Q1 over V vectors laid out one per group of
+// threads.  Stage 0 (radix Q0, Q1 butterflies per vector) writes output q of
+// butterfly j to element j*Q0 + q; stage 1 (radix Q1, span Q0) reads
+// element j + r*Q0.  Both index a [Q1][Q0] array per vector, stored here
+// with rows padded to Q0+1: writes then go to distinct banks, and each
+// thread's addresses are a base plus compile-time offsets.  tile holds
+// splan_mid_size<Plan, V>() float2s and may alias the sources of ld0 and the
+// destinations of stL (the stages synchronise between reads and writes).
+template <class Plan, bool INV, int V, bool GTW, class Ld0, class StL>
+__device__ __forceinline__ void sfft2_rows(const float2* stw, float2* tile, const Ld0& ld0,
+                                           const StL& stL) {
+  constexpr int Q0 = Plan::q(0), Q1 = Plan::q(1);
+  constexpr int RS = Q0 + 1;   // padded row
+  constexpr int VS = Q1 * RS;  // vector
+  const int b = threadIdx.x;
+  {
+    const bool act = b < V * Q1;
+    const int v = b / Q1;
+    const int j = b - v * Q1;
+    float2 x[Q0];
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < Q0; ++r) x[r] = ld0.ld(v, j + r * Q1);
+    }
+    if (Ld0::kSmem) __syncthreads();
+    if (act) {
+      DftS<Q0, INV>::run(x);
+      float2* o = tile + v * VS + j * RS;
+#pragma unroll
+      for (int q = 0; q < Q0; ++q) o[q] = x[q];
+    }
+    __syncthreads();
+  }
+  {
+    const bool act = b < V * Q0;
+    const int v = b / Q0;
+    const int j = b - v * Q0;
+    float2 x[Q1];
+    if (act) {
+      const float2* i = tile + v * VS + j;
+#pragma unroll
+      for (int r = 0; r < Q1; ++r) x[r] = i[r * RS];
+    }
+    if (StL::kSmem) __syncthreads();
+    if (act) {
+      const float2* tw = stw + (Q0 - 1) + j;
+#pragma unroll
+      for (int r = 1; r < Q1; ++r) {
+        const float2 w = GTW ? __ldg(tw + (r - 1) * Q0) : tw[(r - 1) * Q0];
+        x[r] = INV ? cmulconj(x[r], w) : cmul(x[r], w);
+      }
+      DftS<Q1, INV>::run(x);
+      store_group<Q1>(stL, v, j, Q0, x);
+    }
+    if (StL::kSmem) __syncthreads();
+  }
+}
+
 // Full transform; same contract as fft_run (fft_engine.cuh): the first stage
 // reads with ld0, the last writes with stL, the stages between work in place
 // on io; ends with a barrier when stL writes shared memory.
-template <class Plan, bool INV, int V, bool VFAST, class Ld0, class StL>
-__device__ __forceinline__ void sfft_run(const float2* stw, const SmemIO& io, const Ld0& ld0,
+template <class Plan, bool INV, int V, bool VFAST, bool GTW, class IO, class Ld0, class StL>
+__device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const Ld0& ld0,
                                          const StL& stL) {
   constexpr int L = Plan::kL;
   constexpr int N = Plan::kN;
-  if constexpr (N == 1) {
+  static_assert(!GTW || (N == 2 && !VFAST), "global twiddles: two-radix row plans only");
+  if constexpr (N == 2 && !VFAST) {
+    sfft2_rows<Plan, INV, V, GTW>(stw, io.sm, ld0, stL);
+  } else if constexpr (N == 1) {
     sstage<L, Plan::q(0), 1, INV, V, VFAST, true, StL::kSmem>(stw, ld0, stL);
   } else {
     sstage<L, Plan::q(0), 1, INV, V, VFAST, Ld0::kSmem, true>(stw, ld0, io);
@@ -106,8 +185,15 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const SmemIO& io, co
 }
 
 // Runners: the pass kernels are templates over how they transform their tile.
+// Runner::Tile is the natural-order tile type the pass kernels hand to the
+// transform (row tiles: element e of vector v; the generic engine pads it).
 struct GenericRunner {
   static constexpr bool kStatic = false;
+  static constexpr int kV = 0;  // vectors per tile: runtime
+  static constexpr bool kGlobalTw = false;
+  static constexpr int kTileF2 = 0;  // tile size: from the runtime geometry
+  using Tile = SmemIO;
+  __device__ __forceinline__ static Tile row_tile(float2* sm, int L) { return SmemIO{sm, 1, L}; }
   template <bool INV, class Ld0, class StL>
   __device__ __forceinline__ static void run(const FftDev& f, int V, float invV, bool vfast,
                                              const float2* stw, const SmemIO& io, const Ld0& ld0,
@@ -116,14 +202,56 @@ struct GenericRunner {
   }
 };
 
-template <class Plan, int V, bool VFAST>
+// GTW: the stage twiddles are read from the global table (through the
+// read-only cache) instead of a shared-memory copy, which saves the kernel
+// L float2s of shared memory.
+template <class Plan, int V, bool VFAST, bool GTW = false>
 struct StaticRunner {
   static constexpr bool kStatic = true;
-  template <bool INV, class Ld0, class StL>
+  static constexpr int kV = V;
+  static constexpr bool kGlobalTw = GTW;
+  // float2s of a row tile: the middle layout, the natural layout and the
+  // staged half spectra (V vectors of L/2+1 float4) share it
+  static constexpr int kTileF2 = [] {
+    int m = splan_mid_size<Plan, V>();
+    if (V * Plan::kL > m) m = V * Plan::kL;
+    if (2 * (Plan::kL / 2 + 1) * V > m) m = 2 * (Plan::kL / 2 + 1) * V;
+    return m + (m & 1);
+  }();
+  using Tile = NatIO;
+  __device__ __forceinline__ static Tile row_tile(float2* sm, int L) { return NatIO{sm, L}; }
+  template <bool INV, class IO, class Ld0, class StL>
   __device__ __forceinline__ static void run(const FftDev&, int, float, bool, const float2* stw,
-                                             const SmemIO& io, const Ld0& ld0, const StL& stL) {
-    sfft_run<Plan, INV, V, VFAST>(stw, io, ld0, stL);
+                                             const IO& io, const Ld0& ld0, const StL& stL) {
+    sfft_run<Plan, INV, V, VFAST, GTW>(stw, io, ld0, stL);
   }
 };
+
+// Vectors per tile: the runner's compile-time count, else the runtime one
+// (index arithmetic over the tile then divides by a constant).
+template <class Run>
+__device__ __forceinline__ int tile_vectors(int v) {
+  return Run::kV > 0 ? Run::kV : v;
+}
+
+// idx / d and idx % d for 0 <= idx < 2^22: by the constant when D > 0, else
+// through fdiv with the float reciprocal inv_d of the runtime d.
+template <int D>
+__device__ __forceinline__ void divmod_small(int idx, int d, float inv_d, int& q, int& r) {
+  if constexpr (D > 0) {
+    q = idx / D;
+    r = idx - q * D;
+  } else {
+    q = fdiv(idx, inv_d);
+    r = idx - q * d;
+  }
+}
+
+// A static plan's row tile must fit the padded tile the generic sizing gives
+// (spad_size(V*L) float2s), which the pass launchers allocate.
+template <class Plan, int V>
+constexpr bool splan_rows_fit() {
+  return splan_mid_size<Plan, V>() <= spad_size(V * Plan::kL);
+}
 
 }  // namespace cdx

@@ -65,8 +65,9 @@ struct RLWork {
 // Number of blocks of the x passes (= dot-product partials per iteration).
 int x_pass_blocks(const Geom& g);
 // Forward x pass: Y (from X, Xm1, lambda when predict != 0, else Y = X) ->
-// spectrum after the R2C along x.
-int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, const float* Xm1,
+// spectrum after the R2C along x.  When predict != 0, Y = max(X + lam*(X - Xm1), 0)
+// is also written over Xm1 (whose old values are not needed afterwards).
+int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, float* Xm1,
                  const float* lam, int predict, float2* S, cudaStream_t st);
 // In-place complex FFT along y of every (kx, z) row.
 int launch_y_pass(const Geom& g, const FftLen& fy, float2* S, bool inverse, cudaStream_t st);
@@ -78,14 +79,13 @@ int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf,
 // second convolution (spectrum updated in place).
 int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const float* raw,
                            float eps, cudaStream_t st);
-// Inverse x pass followed by the estimate update:
-//   Y = predict ? max(X + lam*(X - Xm1), 0) : X
+// Inverse x pass followed by the estimate update from the prediction Y:
 //   Xnew = max(CC*Y, 0); Gnew = Xnew - Y
-// writes Xnew into Xout (may alias Xm1) and Gnew into G, and when dots != 0
+// writes Xnew into Xout (may alias Y) and Gnew into G, and when dots != 0
 // accumulates (Gnew.Gold, Gold.Gold) and stores the next lambda into lam_next.
-int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* X,
-                        const float* Xm1, const float* lam, int predict, float* Xout, float* G,
-                        int dots, RLWork& w, float* lam_next, float eps, cudaStream_t st);
+int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* Y,
+                        float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
+                        cudaStream_t st);
 // Plain inverse x pass to a real volume (test path).
 int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* out,
                        cudaStream_t st);

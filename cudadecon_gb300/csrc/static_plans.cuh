@@ -32,6 +32,12 @@ namespace cdx {
 CDX_SPLAN_LIST(CDX_DEF_SPLAN)
 #undef CDX_DEF_SPLAN
 
+#define CDX_FIT_ROWS(L, V) \
+  static_assert(splan_rows_fit<SP##L, V>(), "row tile too small for the static plan of length " #L);
+CDX_X_PLANS(CDX_FIT_ROWS)
+CDX_Y_PLANS(CDX_FIT_ROWS)
+#undef CDX_FIT_ROWS
+
 // Radices of the registered plan for length L (false when L is not registered).
 inline bool static_radices(int L, std::vector<int>& rad) {
   switch (L) {
