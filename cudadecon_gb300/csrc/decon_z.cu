@@ -14,64 +14,140 @@ static int z_cols(int nz) {
   return w;
 }
 
+// Last forward stage of the static z pass: multiply element e (= kz) of the
+// thread's column by the OTF, interpolated from the kz-resampled radial
+// table at the column's radius (computed once per thread), or read from the
+// precomputed 3D array.
+template <class IO>
+struct OtfColMulStore {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  IO io;
+  const float2* lo;    // mode 0: table row ir; mode 1: the column of the 3D array
+  const float2* hi;    // mode 0: table row ir + 1
+  float ar;
+  int valid, full, nyp, conj;
+  __device__ __forceinline__ void st(int v, int e, float2 x) const {
+    float2 o = make_float2(0.f, 0.f);
+    if (full) {
+      o = __ldg(lo + (long long)e * nyp);
+    } else if (valid) {
+      const float2 t0 = __ldg(lo + e), t1 = __ldg(hi + e);
+      o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+    }
+    io.st(v, e, conj ? cmulconj(x, o) : cmul(x, o));
+  }
+};
+
 template <class Run>
 __global__ void __launch_bounds__(kMaxThreads, 1)
 k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int Wa) {
   const int W = tile_vectors<Run>(Wa);
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(16) float2 smem[];
   const int nz = g.nz;
   const int kx = blockIdx.y;
   const int y0 = blockIdx.x * W;
   float2* stw = smem;
-  const SmemIO io{smem + nz, W, 1};
-  float2* otf_tile = smem + nz + spad_size(W * nz);
-  load_twiddles(fz, stw);
   const float invW = 1.f / (float)W;
   const SpecColIO gio{S + (long long)kx * g.plane, y0, g.ny, g.nyp};
-  if (fwd_only) {
-    __syncthreads();
-    Run::template run<false>(fz, W, invW, true, stw, io, gio, gio);
-    return;
-  }
-  // OTF of every (y, z) of the tile, interpolated on the fly from the
-  // kz-resampled radial table (dev_otfinterpolate RA branch,
-  // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
-  // read from the precomputed 3D array
-  for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-    int w, z;
-    divmod_small<Run::kV>(idx, W, invW, z, w);
-    const int y = y0 + w;
-    float2 o = make_float2(0.f, 0.f);
-    if (y < g.ny) {
-      if (otf.mode == 1) {
-        o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
-      } else {
-        const int ky = y > (g.ny >> 1) ? y - g.ny : y;
-        const float fx = (float)kx * otf.kxscale;
-        const float fy = (float)ky * otf.kyscale;
-        const float kr = sqrtf(fx * fx + fy * fy);
-        if (kr < (float)(otf.nr - 1)) {
-          const int ir = (int)floorf(kr);
-          const float ar = kr - (float)ir;
-          const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
-          const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
-          o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
-        }
+  if constexpr (Run::kStatic) {
+    // The tile (W columns of nz elements, interleaved) is copied with
+    // cp.async: one contiguous run of W complex values per z.
+    const auto io = Run::col_tile(smem + (nz + (nz & 1)), W);
+    constexpr int kChunks = Run::kV / 2;  // 16-byte chunks per z row
+    const float2* src = S + (long long)kx * g.plane + y0;
+    for (int idx = threadIdx.x; idx < nz * kChunks; idx += blockDim.x) {
+      const int z = idx / kChunks;
+      const int c = idx - z * kChunks;
+      if (y0 + 2 * c < g.ny) cp_async16(io.sm + z * W + 2 * c, src + (long long)z * g.nyp + 2 * c);
+    }
+    cp_async_commit();
+    // the OTF of this thread's column (the column is fixed across stages)
+    const int v = threadIdx.x % Run::kV;
+    const int y = y0 + v;
+    const float2* lo = otf.tz;
+    const float2* hi = otf.tz;
+    float ar = 0.f;
+    int valid = 0;
+    if (otf.mode == 1) {
+      lo = otf.full + (long long)kx * g.plane + (y < g.ny ? y : 0);
+    } else if (y < g.ny) {
+      // dev_otfinterpolate RA branch (RLgpuImpl.cu:238-273): kr = sqrt(kx^2 +
+      // ky^2), zero at kr >= nr-1
+      const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+      const float fx = (float)kx * otf.kxscale;
+      const float fy = (float)ky * otf.kyscale;
+      const float kr = sqrtf(fx * fx + fy * fy);
+      if (kr < (float)(otf.nr - 1)) {
+        const int ir = (int)floorf(kr);
+        ar = kr - (float)ir;
+        lo = otf.tz + (long long)ir * nz;
+        hi = lo + nz;
+        valid = 1;
       }
     }
-    otf_tile[idx] = o;
+    load_twiddles(fz, stw);
+    cp_async_wait_all();
+    __syncthreads();
+    if (fwd_only) {
+      Run::template run<false>(fz, W, invW, true, stw, io, io, gio);
+      return;
+    }
+    const OtfColMulStore<decltype(io)> ost{io, lo, hi, ar, valid, otf.mode == 1, g.nyp, conj};
+    Run::template run<false>(fz, W, invW, true, stw, io, io, ost);
+    Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
+  } else {
+    const SmemIO io{smem + nz, W, 1};
+    float2* otf_tile = smem + nz + spad_size(W * nz);
+    load_twiddles(fz, stw);
+    if (fwd_only) {
+      __syncthreads();
+      Run::template run<false>(fz, W, invW, true, stw, io, gio, gio);
+      return;
+    }
+    // OTF of every (y, z) of the tile, interpolated on the fly from the
+    // kz-resampled radial table (dev_otfinterpolate RA branch,
+    // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
+    // read from the precomputed 3D array
+    for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
+      int w, z;
+      divmod_small<Run::kV>(idx, W, invW, z, w);
+      const int y = y0 + w;
+      float2 o = make_float2(0.f, 0.f);
+      if (y < g.ny) {
+        if (otf.mode == 1) {
+          o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
+        } else {
+          const int ky = y > (g.ny >> 1) ? y - g.ny : y;
+          const float fx = (float)kx * otf.kxscale;
+          const float fy = (float)ky * otf.kyscale;
+          const float kr = sqrtf(fx * fx + fy * fy);
+          if (kr < (float)(otf.nr - 1)) {
+            const int ir = (int)floorf(kr);
+            const float ar = kr - (float)ir;
+            const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
+            const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
+            o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+          }
+        }
+      }
+      otf_tile[idx] = o;
+    }
+    __syncthreads();
+    const OtfMulStore ost{io, otf_tile, W, conj};
+    Run::template run<false>(fz, W, invW, true, stw, io, gio, ost);
+    Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
   }
-  __syncthreads();
-  const OtfMulStore ost{io, otf_tile, W, conj};
-  Run::template run<false>(fz, W, invW, true, stw, io, gio, ost);
-  Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
 }
 
 template <class Run>
 static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bool conj,
                 bool fwd_only, int W, int T, cudaStream_t st) {
   dim3 grid(ceil_div(g.ny, W), g.nxh);
-  size_t smem = fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
+  // static: twiddles + unpadded tile; generic: twiddles + padded tile + OTF tile
+  size_t smem = Run::kStatic
+                    ? sizeof(float2) * ((size_t)(g.nz + (g.nz & 1)) + (size_t)W * g.nz)
+                    : fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
   if (int rc = smem_optin(k_z_pass<Run>, smem)) return rc;
   k_z_pass<Run><<<grid, T, smem, st>>>(g, f, S, otf, conj ? 1 : 0, fwd_only ? 1 : 0, W);
   CDX_LAUNCH_CHECK("k_z_pass");

@@ -161,6 +161,69 @@ __device__ __forceinline__ void sfft2_rows(const float2* stw, float2* tile, cons
   }
 }
 
+// Interleaved tile of V columns: element e of column v at sm[e * V + v].
+// Consecutive threads own consecutive columns, so every access of a stage
+// touches V consecutive float2s and the tile needs no padding.
+template <int V>
+struct ColIO {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  float2* sm;
+  __device__ __forceinline__ float2 ld(int v, int e) const { return sm[e * V + v]; }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[e * V + v] = x; }
+};
+
+// Two-radix transform over V interleaved columns (thread b owns column
+// b % V).  Same stage arithmetic as sfft2_rows; the middle array is stored
+// interleaved like the tile ([Q1][Q0] per column, column fastest).
+template <class Plan, bool INV, int V, class Ld0, class StL>
+__device__ __forceinline__ void sfft2_cols(const float2* stw, float2* tile, const Ld0& ld0,
+                                           const StL& stL) {
+  constexpr int Q0 = Plan::q(0), Q1 = Plan::q(1);
+  const int b = threadIdx.x;
+  {
+    const bool act = b < V * Q1;
+    const int j = b / V;
+    const int v = b - j * V;
+    float2 x[Q0];
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < Q0; ++r) x[r] = ld0.ld(v, j + r * Q1);
+    }
+    if (Ld0::kSmem) __syncthreads();
+    if (act) {
+      DftS<Q0, INV>::run(x);
+      float2* o = tile + (j * Q0) * V + v;
+#pragma unroll
+      for (int q = 0; q < Q0; ++q) o[q * V] = x[q];
+    }
+    __syncthreads();
+  }
+  {
+    const bool act = b < V * Q0;
+    const int j = b / V;
+    const int v = b - j * V;
+    float2 x[Q1];
+    if (act) {
+      const float2* i = tile + j * V + v;
+#pragma unroll
+      for (int r = 0; r < Q1; ++r) x[r] = i[r * Q0 * V];
+    }
+    if (StL::kSmem) __syncthreads();
+    if (act) {
+      const float2* tw = stw + (Q0 - 1) + j;
+#pragma unroll
+      for (int r = 1; r < Q1; ++r) {
+        const float2 w = tw[(r - 1) * Q0];
+        x[r] = INV ? cmulconj(x[r], w) : cmul(x[r], w);
+      }
+      DftS<Q1, INV>::run(x);
+      store_group<Q1>(stL, v, j, Q0, x);
+    }
+    if (StL::kSmem) __syncthreads();
+  }
+}
+
 // Full transform; same contract as fft_run (fft_engine.cuh): the first stage
 // reads with ld0, the last writes with stL, the stages between work in place
 // on io; ends with a barrier when stL writes shared memory.
@@ -172,6 +235,8 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const 
   static_assert(!GTW || (N == 2 && !VFAST), "global twiddles: two-radix row plans only");
   if constexpr (N == 2 && !VFAST) {
     sfft2_rows<Plan, INV, V, GTW>(stw, io.sm, ld0, stL);
+  } else if constexpr (N == 2) {
+    sfft2_cols<Plan, INV, V>(stw, io.sm, ld0, stL);
   } else if constexpr (N == 1) {
     sstage<L, Plan::q(0), 1, INV, V, VFAST, true, StL::kSmem>(stw, ld0, stL);
   } else {
@@ -194,6 +259,7 @@ struct GenericRunner {
   static constexpr int kTileF2 = 0;  // tile size: from the runtime geometry
   using Tile = SmemIO;
   __device__ __forceinline__ static Tile row_tile(float2* sm, int L) { return SmemIO{sm, 1, L}; }
+  __device__ __forceinline__ static SmemIO col_tile(float2* sm, int W) { return SmemIO{sm, W, 1}; }
   template <bool INV, class Ld0, class StL>
   __device__ __forceinline__ static void run(const FftDev& f, int V, float invV, bool vfast,
                                              const float2* stw, const SmemIO& io, const Ld0& ld0,
@@ -220,6 +286,7 @@ struct StaticRunner {
   }();
   using Tile = NatIO;
   __device__ __forceinline__ static Tile row_tile(float2* sm, int L) { return NatIO{sm, L}; }
+  __device__ __forceinline__ static ColIO<V> col_tile(float2* sm, int) { return ColIO<V>{sm}; }
   template <bool INV, class IO, class Ld0, class StL>
   __device__ __forceinline__ static void run(const FftDev&, int, float, bool, const float2* stw,
                                              const IO& io, const Ld0& ld0, const StL& stL) {
