@@ -279,30 +279,40 @@ int mean_above_background(const float* img, long long n, double* d_tmp, unsigned
 // nvcc build evaluates it (pinned against the reference kernel on the GPU):
 // the source coordinate in double with one fused multiply-add, rounded once
 // to float; the blend (1-offset)*a + offset*b with the first product fused.
+// The source coordinate depends on (xout, zout) only, so each thread
+// evaluates it once (in double, as the reference does per voxel) and then
+// walks kGeomRows rows of y; GB300's FP64 rate is a small fraction of its
+// FP32 rate.
+constexpr int kGeomRows = 16;
+
 __global__ void k_deskew(const float* __restrict__ in, int nx, int ny, int nz,
                          float* __restrict__ out, int nxOut, int extraShift, double deskewFactor,
                          float padVal) {
   const unsigned xout = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned yout = blockIdx.y;
-  const unsigned zout = blockIdx.z;
+  const unsigned zout = blockIdx.y;
+  const unsigned y0 = blockIdx.z * kGeomRows;
   if (xout >= (unsigned)nxOut) return;
   const double a = __dadd_rn(__dsub_rn((double)xout, nxOut / 2.), (double)extraShift);
   const double b = __dsub_rn((double)zout, nz / 2.);
   const float xin = __double2float_rn(__dadd_rn(__fma_rn(-deskewFactor, b, a), nx / 2.));
-  const size_t indout = ((size_t)zout * ny + yout) * nxOut + xout;
+  const unsigned y1 = min(y0 + kGeomRows, (unsigned)ny);
   if (xin >= 0 && xin < nx - 1) {
     const float fl = floorf(xin);
-    const size_t indin = ((size_t)zout * ny + yout) * nx + (unsigned int)fl;
     const float offset = __fsub_rn(xin, fl);
-    out[indout] = __fmaf_rn(__fsub_rn(1.f, offset), in[indin], __fmul_rn(offset, in[indin + 1]));
+    const float w0 = __fsub_rn(1.f, offset);
+    for (unsigned y = y0; y < y1; ++y) {
+      const size_t indin = ((size_t)zout * ny + y) * nx + (unsigned int)fl;
+      out[((size_t)zout * ny + y) * nxOut + xout] =
+          __fmaf_rn(w0, __ldg(in + indin), __fmul_rn(offset, __ldg(in + indin + 1)));
+    }
   } else {
-    out[indout] = padVal;
+    for (unsigned y = y0; y < y1; ++y) out[((size_t)zout * ny + y) * nxOut + xout] = padVal;
   }
 }
 
 int launch_deskew(const float* in, int nx, int ny, int nz, double deskewFactor, float* out,
                   int nxOut, int extraShift, float padVal, cudaStream_t st) {
-  dim3 grid(ceil_div(nxOut, 128), ny, nz);
+  dim3 grid(ceil_div(nxOut, 128), nz, ceil_div(ny, kGeomRows));
   k_deskew<<<grid, 128, 0, st>>>(in, nx, ny, nz, out, nxOut, extraShift, deskewFactor, padVal);
   CDX_LAUNCH_CHECK("k_deskew");
   return 0;
@@ -323,8 +333,8 @@ struct Rot4 {
 __global__ void k_rotate(const float* __restrict__ in, int nx_in, int ny, int nz_in,
                          float* __restrict__ out, int nx_out, int nz_out, Rot4 rot) {
   const unsigned xout = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned yout = blockIdx.y;
-  const unsigned zout = blockIdx.z;
+  const unsigned zout = blockIdx.y;
+  const unsigned y0 = blockIdx.z * kGeomRows;
   if (xout >= (unsigned)nx_out) return;
   const float xc = __double2float_rn(__dsub_rn((double)xout, nx_out / 2.));
   const float zc = __double2float_rn(__dsub_rn((double)zout, nz_out / 2.));
@@ -334,18 +344,22 @@ __global__ void k_rotate(const float* __restrict__ in, int nx_in, int ny, int nz
       __dadd_rn((double)__fmaf_rn(rot.p[2], zc, __fmul_rn(rot.p[3], xc)), nx_in / 2.));
   const size_t nxy_in = (size_t)nx_in * ny;
   const size_t nxy_out = (size_t)nx_out * ny;
-  const size_t indout = (size_t)(nz_out - 1 - zout) * nxy_out + (size_t)yout * nx_out + xout;
+  const size_t obase = (size_t)(nz_out - 1 - zout) * nxy_out + xout;
+  const unsigned y1 = min(y0 + kGeomRows, (unsigned)ny);
   if (xin >= 0 && xin < nx_in - 1 && zin >= 0 && zin < nz_in - 1) {
     const float fz = floorf(zin), fx = floorf(xin);
-    const size_t i00 = (size_t)(unsigned)fz * nxy_in + (size_t)yout * nx_in + (unsigned)fx;
-    const size_t i01 = i00 + 1, i10 = i00 + nxy_in, i11 = i10 + 1;
+    const size_t ibase = (size_t)(unsigned)fz * nxy_in + (unsigned)fx;
     const float xo = __fsub_rn(xin, fx), zo = __fsub_rn(zin, fz);
     const float wx = __fsub_rn(1.f, xo), wz = __fsub_rn(1.f, zo);
-    const float a = __fmaf_rn(wx, in[i00], __fmul_rn(xo, in[i01]));
-    const float b = __fmaf_rn(wx, in[i10], __fmul_rn(xo, in[i11]));
-    out[indout] = __fmaf_rn(wz, a, __fmul_rn(zo, b));
+    for (unsigned y = y0; y < y1; ++y) {
+      const size_t i00 = ibase + (size_t)y * nx_in;
+      const size_t i10 = i00 + nxy_in;
+      const float a = __fmaf_rn(wx, __ldg(in + i00), __fmul_rn(xo, __ldg(in + i00 + 1)));
+      const float b = __fmaf_rn(wx, __ldg(in + i10), __fmul_rn(xo, __ldg(in + i10 + 1)));
+      out[obase + (size_t)y * nx_out] = __fmaf_rn(wz, a, __fmul_rn(zo, b));
+    }
   } else {
-    out[indout] = 0.f;
+    for (unsigned y = y0; y < y1; ++y) out[obase + (size_t)y * nx_out] = 0.f;
   }
 }
 
@@ -353,7 +367,7 @@ int launch_rotate(const float* in, int nx_in, int ny, int nz_in, const float* ro
                   int nx_out, int nz_out, cudaStream_t st) {
   Rot4 r;
   for (int i = 0; i < 4; ++i) r.p[i] = rot_host[i];
-  dim3 grid(ceil_div(nx_out, 128), ny, nz_out);
+  dim3 grid(ceil_div(nx_out, 128), nz_out, ceil_div(ny, kGeomRows));
   k_rotate<<<grid, 128, 0, st>>>(in, nx_in, ny, nz_in, out, nx_out, nz_out, r);
   CDX_LAUNCH_CHECK("k_rotate");
   return 0;
