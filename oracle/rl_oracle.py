@@ -15,10 +15,13 @@ the same unnormalised DFT, so only rounding differs.
 dtype=np.float32 reproduces the reference's single-precision iteration;
 dtype=np.float64 is the FP64 oracle the precision targets are measured against.
 
-Parity status: this restatement has no golden vectors from the reference to
-be checked against (the reference ships none); it is pinned by running the
-reference's own kernels on the GPU (tests/test_ref_pin.py) when their build
-is present.
+Parity status: pinned.  The reference ships no golden vectors, so its own
+CUDA kernels (compiled from its sources by oracle/build.py) were run with
+cuFFT on a GB300 through oracle/ref_runner.cu: deskew, rotate, camcor and
+affine outputs and two RL runs (64x256x256 plain; 100x256x756 deskewed stage
+scan) are committed as fixtures in tests/golden/ (tests/golden/make_golden.py),
+and tests/test_golden_cpu.py checks this restatement against them.
+tests/test_ref_pin.py repeats the comparison live when that build is present.
 """
 
 from __future__ import annotations
