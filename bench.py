@@ -164,6 +164,17 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
+def max_over_ranks(x, pg, device="cpu"):
+    """Largest x over all ranks (the slowest rank's time); x itself without a group.
+    The tensor lives on `device` (CPU for gloo, the rank's GPU for nccl)."""
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
@@ -250,11 +261,7 @@ def run_gb300(args):
     torch.cuda.synchronize()
     dev_ms = e0.elapsed_time(e1)
     clocks = clk.stop()
-    if pg:
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    dev_ms = max_over_ranks(dev_ms, pg, dev)
     ms_per_step = dev_ms / args.steps
     vox_iters = grid_vox * n_iters
     value = world * vox_iters / (ms_per_step / 1000.0)
@@ -273,7 +280,10 @@ def run_gb300(args):
     L.cdx_profile_read(pm, pn, 9, ctypes.byref(it_ms), ctypes.byref(it_n))
     L.cdx_profile_enable(0)
     iter_ms = it_ms.value / max(it_n.value, 1)
-    pass_bytes = [12, 8, 8, 8, 12, 8, 8, 8, 24]  # bytes per voxel moved by each pass as built
+    # bytes per voxel moved by each pass as built: x forward reads X, X_{k-1} and
+    # writes the spectrum and the prediction Y; x update reads the spectrum, Y
+    # and G_{k-1} and writes X_{k+1} and G_k
+    pass_bytes = [16, 8, 8, 8, 12, 8, 8, 8, 20]
     passes = {}
     for i in range(9):
         ms = pm[i] / max(pn[i], 1)
@@ -308,10 +318,7 @@ def run_gb300(args):
     for _ in range(args.steps):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if pg:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, pg, dev)
     e2e_val = world * vox_iters / e2e_s
 
     cpu = None
