@@ -19,6 +19,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _build
+from . import synth
 
 __all__ = [
     "lib",
@@ -57,6 +58,14 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
 _F = POINTER(c_float)
 _U16 = POINTER(c_ushort)
+
+
+class BatchStack(ctypes.Structure):
+    """struct cdx_batch_stack of include/cudadecon.h."""
+    _fields_ = [("raw", c_void_p), ("nx", c_int), ("ny", c_int), ("nz", c_int),
+                ("result", c_void_p), ("otf", _F), ("otf_w", c_int), ("otf_h", c_int),
+                ("dr", c_float), ("dz", c_float), ("dr_psf", c_float), ("dz_psf", c_float),
+                ("background", c_float)]
 
 
 def _bind(L) -> None:
@@ -103,6 +112,11 @@ def _bind(L) -> None:
                                             c_void_p]),
         "cdx_load_image": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), POINTER(c_int), _F,
                                    c_size_t]),
+        "cdx_batch_grid": (c_int, [c_int, c_int, c_int, POINTER(c_int), POINTER(c_int),
+                                   POINTER(c_int)]),
+        "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
+        "cdx_batch_last_launch_count": (c_longlong, []),
+        "cdx_batch_release": (None, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -188,6 +202,46 @@ def rl_decon(raw: np.ndarray, background=100.0, n_iters=10, rescale=False, save_
 
 def rl_cleanup() -> None:
     lib().RL_cleanup()
+
+
+def batch_grid(shape_zyx):
+    """(gz, gy, gx): the decon grid cdx_RL_batch_device uses for a stack."""
+    nz, ny, nx = shape_zyx
+    g = [c_int(0), c_int(0), c_int(0)]
+    lib().cdx_batch_grid(nx, ny, nz, *(ctypes.byref(v) for v in g))
+    return g[2].value, g[1].value, g[0].value
+
+
+def rl_batch(stacks, n_iters=10, stream=None):
+    """cdx_RL_batch_device on a list of stacks.  Each stack is a dict with
+    `raw` (CUDA uint16 tensor, (nz, ny, nx)), `otf` ((nr, nz_otf) complex64
+    radial table, host), `dr`, `dz`, `dr_psf`, `dz_psf` and `background`.
+    Returns the float32 results (CUDA tensors on each stack's decon grid),
+    complete when the work queued on `stream` (default: the current stream)
+    after this call runs."""
+    import torch
+    L = lib()
+    n = len(stacks)
+    arr = (BatchStack * n)()
+    keep, outs = [], []
+    for i, d in enumerate(stacks):
+        raw = d["raw"]
+        nz, ny, nx = raw.shape
+        gz, gy, gx = batch_grid((nz, ny, nx))
+        out = torch.empty((gz, gy, gx), dtype=torch.float32, device=raw.device)
+        img = np.ascontiguousarray(synth.otf_table_to_image(d["otf"]), dtype=np.float32)
+        keep.append(img)
+        outs.append(out)
+        arr[i] = BatchStack(raw.data_ptr(), nx, ny, nz, out.data_ptr(), _fptr(img), img.shape[1],
+                            img.shape[0], d.get("dr", 0.104), d.get("dz", 0.3),
+                            d.get("dr_psf", 0.104), d.get("dz_psf", 0.1),
+                            d.get("background", 100.0))
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    ok = L.cdx_RL_batch_device(arr, n, int(n_iters), c_void_p(stream.cuda_stream))
+    if ok != 1:
+        _err("cdx_RL_batch_device")
+    return outs
 
 
 # ---------------------------------------------------------------- geometry

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -227,12 +228,77 @@ static int ensure_stream(Session& s) {
   return 0;
 }
 
-// Build (or reuse) FFT plans and the OTF table for a decon grid (gx, gy, gz).
-// The OTF k-scales follow RL_interface_init (RL-Biggs-Andrews.cpp:634-642):
-// dk = 1/(pixel * size) per axis divided by the OTF's dk.
-static int ensure_plan(Session& s, int gx, int gy, int gz) {
-  GridPlan& p = s.plan;
-  if (p.valid && p.g.nx == gx && p.g.ny == gy && p.g.nz == gz) return 0;
+// OTF description shared by the session and the batch stacks: the raw table
+// on the device, its dimensions and k-steps (determine_OTF_dimensions,
+// RL-Biggs-Andrews.cpp:506-529; dk values of RL_interface_init 576-590).
+struct OtfSpec {
+  RawOtfDims od{};
+  float dkx_otf = 0, dky_otf = 0, dkz_otf = 0;
+  const float2* raw_otf = nullptr;
+};
+
+// OTF dimensions and k-steps from a table of w x h x d floats (width 2*nz_otf
+// for radial tables); false when the table is too small.
+static bool otf_spec_dims(int w, int h, int d, float dr_psf, float dz_psf, OtfSpec& o) {
+  unsigned nx_otf, ny_otf, nz_otf;
+  if (d > 1) {
+    nx_otf = w / 2;
+    ny_otf = h;
+    nz_otf = d;
+  } else {
+    nx_otf = h;
+    ny_otf = 1;
+    nz_otf = w / 2;
+  }
+  if (nx_otf < 2 || nz_otf < 1) return false;
+  o.dkx_otf = 1 / ((nx_otf - 1) * 2 * dr_psf);
+  o.dky_otf = ny_otf > 1 ? 1 / (ny_otf * dr_psf) : o.dkx_otf;
+  o.dkz_otf = 1 / (nz_otf * dz_psf);
+  o.od.nx_otf = nx_otf;
+  o.od.ny_otf = ny_otf;
+  o.od.nz_otf = nz_otf;
+  return true;
+}
+
+// OTF table of a plan from the raw table o.raw_otf: the kz-resampled radial
+// table (scaled by 1/N) or, for 3D OTF files, the full spectrum-layout array.
+static int fill_otf(GridPlan& p, float dr, float dz, const OtfSpec& o, cudaStream_t st) {
+  const int gx = p.g.nx, gy = p.g.ny, gz = p.g.nz;
+  const float dkx = 1.0 / (dr * (unsigned)gx);
+  const float dky = 1.0 / (dr * (unsigned)gy);
+  const float dkz = 1.0 / (dz * (unsigned)gz);
+  RawOtfDims od = o.od;
+  od.kxscale = dkx / o.dkx_otf;
+  od.kyscale = dky / o.dky_otf;
+  od.kzscale = dkz / o.dkz_otf;
+  const float scale = (float)(1.0 / ((double)gx * gy * gz));
+  p.otf.nr = od.nx_otf;
+  p.otf.kxscale = od.kxscale;
+  p.otf.kyscale = od.kyscale;
+  p.otf.tz = nullptr;
+  p.otf.full = nullptr;
+  int rc;
+  if (od.ny_otf == 1) {
+    p.otf.mode = 0;
+    if ((rc = p.tz.ensure((size_t)od.nx_otf * gz))) return rc;
+    if ((rc = launch_otf_tz(p.g, o.raw_otf, od, p.tz.p, scale, st))) return rc;
+    p.otf.tz = p.tz.p;
+  } else {
+    p.otf.mode = 1;
+    if ((rc = p.full.ensure((size_t)p.g.spec_elems()))) return rc;
+    if ((rc = launch_otf_full(p.g, o.raw_otf, od, p.full.p, scale, st))) return rc;
+    p.otf.full = p.full.p;
+  }
+  p.valid = true;
+  return 0;
+}
+
+// Build FFT plans and the OTF table for a decon grid (gx, gy, gz).  The OTF
+// k-scales follow RL_interface_init (RL-Biggs-Andrews.cpp:634-642): dk =
+// 1/(pixel * size) per axis divided by the OTF's dk.  Enqueued on st; the
+// caller synchronises before the plan is used from another stream.
+static int build_plan(GridPlan& p, int gx, int gy, int gz, float dr, float dz, const OtfSpec& o,
+                      cudaStream_t st) {
   p.release();
   if (!fft_len_supported(gx) || !fft_len_supported(gy) || !fft_len_supported(gz)) {
     set_error("plan", "decon grid size is not a product of 2, 3, 5 and 7");
@@ -243,32 +309,22 @@ static int ensure_plan(Session& s, int gx, int gy, int gz) {
   if ((rc = fft_len_init(p.fx, gx))) return rc;
   if ((rc = fft_len_init(p.fy, gy))) return rc;
   if ((rc = fft_len_init(p.fz, gz))) return rc;
-  const float dkx = 1.0 / (s.dr * (unsigned)gx);
-  const float dky = 1.0 / (s.dr * (unsigned)gy);
-  const float dkz = 1.0 / (s.dz * (unsigned)gz);
-  RawOtfDims od = s.od;
-  od.kxscale = dkx / s.dkx_otf;
-  od.kyscale = dky / s.dky_otf;
-  od.kzscale = dkz / s.dkz_otf;
-  const float scale = (float)(1.0 / ((double)gx * gy * gz));
-  p.otf.nr = od.nx_otf;
-  p.otf.kxscale = od.kxscale;
-  p.otf.kyscale = od.kyscale;
-  p.otf.tz = nullptr;
-  p.otf.full = nullptr;
-  if (od.ny_otf == 1) {
-    p.otf.mode = 0;
-    if ((rc = p.tz.ensure((size_t)od.nx_otf * gz))) return rc;
-    if ((rc = launch_otf_tz(p.g, s.raw_otf.p, od, p.tz.p, scale, s.stream))) return rc;
-    p.otf.tz = p.tz.p;
-  } else {
-    p.otf.mode = 1;
-    if ((rc = p.full.ensure((size_t)p.g.spec_elems()))) return rc;
-    if ((rc = launch_otf_full(p.g, s.raw_otf.p, od, p.full.p, scale, s.stream))) return rc;
-    p.otf.full = p.full.p;
-  }
+  return fill_otf(p, dr, dz, o, st);
+}
+
+// Session plan for a decon grid (reused while the grid does not change).
+static int ensure_plan(Session& s, int gx, int gy, int gz) {
+  GridPlan& p = s.plan;
+  if (p.valid && p.g.nx == gx && p.g.ny == gy && p.g.nz == gz) return 0;
+  OtfSpec o;
+  o.od = s.od;
+  o.dkx_otf = s.dkx_otf;
+  o.dky_otf = s.dky_otf;
+  o.dkz_otf = s.dkz_otf;
+  o.raw_otf = s.raw_otf.p;
+  int rc;
+  if ((rc = build_plan(p, gx, gy, gz, s.dr, s.dz, o, s.stream))) return rc;
   CDX_CHECK(cudaStreamSynchronize(s.stream));
-  p.valid = true;
   return 0;
 }
 
@@ -291,61 +347,79 @@ static int ensure_grid_buffers(Session& s, const Geom& g) {
 // The iteration loop of RichardsonLucy_GPU (RL-Biggs-Andrews.cpp:282-367) on
 // the grid of s.plan, starting from X0 in s.Xa with raw in s.raw.  Returns
 // the buffer that holds the final estimate.
-static int rl_iterations(Session& s, int nIter, float** final_x) {
-  const GridPlan& p = s.plan;
+// Device buffers of one RL loop: estimates (X0 in Xa), raw, G, spectrum,
+// dot-product partials, last-block ticket and the two lambda slots.
+struct LoopBufs {
+  float* Xa;
+  float* Xb;
+  float* G;
+  float* raw;
+  float2* S;
+  double* partials;
+  unsigned* counter;
+  float* lam;
+  int max_blocks;
+};
+
+static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t st, bool prof,
+                   float** final_x, long long* launches) {
   const Geom& g = p.g;
   RLWork w;
-  w.partials = s.partials.p;
-  w.counter = s.counter.p;
-  w.lam = s.lam.p;
-  w.max_blocks = (int)(s.partials.n / 2);
+  w.partials = b.partials;
+  w.counter = b.counter;
+  w.lam = b.lam;
+  w.max_blocks = b.max_blocks;
   const float eps = 1.1920928955078125e-07f;  // std::numeric_limits<float>::epsilon()
-  float* X = s.Xa.p;
-  float* Xm1 = s.Xb.p;
+  float* X = b.Xa;
+  float* Xm1 = b.Xb;
   int rc;
-  const bool prof = g_prof.on;
   auto mark = [&]() {
     if (prof) {
       cudaEvent_t e = prof_event();
-      if (e) cudaEventRecord(e, s.stream);
+      if (e) cudaEventRecord(e, st);
     }
   };
   for (int k = 0; k < nIter; ++k) {
     const int predict = k > 1;
-    float* lam_k = s.lam.p + (k & 1);
-    float* lam_n = s.lam.p + ((k + 1) & 1);
+    float* lam_k = b.lam + (k & 1);
+    float* lam_n = b.lam + ((k + 1) & 1);
     mark();
-    if ((rc = launch_x_fwd(g, p.fx, X, Xm1, lam_k, predict, s.S.p, s.stream))) return rc;
+    if ((rc = launch_x_fwd(g, p.fx, X, Xm1, lam_k, predict, b.S, st))) return rc;
     mark();
-    if ((rc = launch_y_pass(g, p.fy, s.S.p, false, s.stream))) return rc;
+    if ((rc = launch_y_pass(g, p.fy, b.S, false, st))) return rc;
     mark();
-    if ((rc = launch_z_pass(g, p.fz, s.S.p, p.otf, false, s.stream))) return rc;
+    if ((rc = launch_z_pass(g, p.fz, b.S, p.otf, false, st))) return rc;
     mark();
-    if ((rc = launch_y_pass(g, p.fy, s.S.p, true, s.stream))) return rc;
+    if ((rc = launch_y_pass(g, p.fy, b.S, true, st))) return rc;
     mark();
-    if ((rc = launch_x_inv_ratio_fwd(g, p.fx, s.S.p, s.raw.p, eps, s.stream))) return rc;
+    if ((rc = launch_x_inv_ratio_fwd(g, p.fx, b.S, b.raw, eps, st))) return rc;
     mark();
-    if ((rc = launch_y_pass(g, p.fy, s.S.p, false, s.stream))) return rc;
+    if ((rc = launch_y_pass(g, p.fy, b.S, false, st))) return rc;
     mark();
-    if ((rc = launch_z_pass(g, p.fz, s.S.p, p.otf, true, s.stream))) return rc;
+    if ((rc = launch_z_pass(g, p.fz, b.S, p.otf, true, st))) return rc;
     mark();
-    if ((rc = launch_y_pass(g, p.fy, s.S.p, true, s.stream))) return rc;
+    if ((rc = launch_y_pass(g, p.fy, b.S, true, st))) return rc;
     mark();
     // x_fwd wrote the prediction Y over Xm1 when predicting (else Y = X);
     // the new estimate replaces it in place
     const float* Y = predict ? Xm1 : X;
-    if ((rc = launch_x_inv_update(g, p.fx, s.S.p, Y, Xm1, s.G.p, k >= 1, w, lam_n, eps,
-                                  s.stream)))
+    if ((rc = launch_x_inv_update(g, p.fx, b.S, Y, Xm1, b.G, k >= 1, w, lam_n, eps, st)))
       return rc;
     mark();
     if (prof && g_prof.used >= 10 * 64) prof_collect();
-    s.launches += 9;
+    *launches += 9;
     float* t = X;
     X = Xm1;
     Xm1 = t;
   }
   *final_x = X;
   return 0;
+}
+
+static int rl_iterations(Session& s, int nIter, float** final_x) {
+  const LoopBufs b{s.Xa.p, s.Xb.p, s.G.p, s.raw.p, s.S.p, s.partials.p, s.counter.p, s.lam.p,
+                   (int)(s.partials.n / 2)};
+  return rl_loop(s.plan, b, nIter, s.stream, g_prof.on, final_x, &s.launches);
 }
 
 struct RLArgs {
@@ -555,27 +629,16 @@ static int init_session(Session& s, int nx, int ny, int nz, float dr, float dz, 
     return cudaErrorInvalidValue;
   }
   if (bSkewedDecon) dz_psf *= fabs(sin(deskewAngle * M_PI / 180.));
-  // determine_OTF_dimensions (RL-Biggs-Andrews.cpp:506-529)
-  unsigned nx_otf, ny_otf, nz_otf;
-  if (otf.d > 1) {
-    nx_otf = otf.w / 2;
-    ny_otf = otf.h;
-    nz_otf = otf.d;
-  } else {
-    nx_otf = otf.h;
-    ny_otf = 1;
-    nz_otf = otf.w / 2;
-  }
-  if (nx_otf < 2 || nz_otf < 1) {
+  OtfSpec os;
+  if (!otf_spec_dims(otf.w, otf.h, otf.d, dr_psf, dz_psf, os)) {
     set_error("RL_interface_init", "OTF too small");
     return cudaErrorInvalidValue;
   }
-  s.dkx_otf = 1 / ((nx_otf - 1) * 2 * dr_psf);
-  s.dky_otf = ny_otf > 1 ? 1 / (ny_otf * dr_psf) : s.dkx_otf;
-  s.dkz_otf = 1 / (nz_otf * dz_psf);
-  s.od.nx_otf = nx_otf;
-  s.od.ny_otf = ny_otf;
-  s.od.nz_otf = nz_otf;
+  s.dkx_otf = os.dkx_otf;
+  s.dky_otf = os.dky_otf;
+  s.dkz_otf = os.dkz_otf;
+  s.od = os.od;
+  const unsigned nx_otf = os.od.nx_otf, ny_otf = os.od.ny_otf, nz_otf = os.od.nz_otf;
   int rc;
   if ((rc = ensure_stream(s))) return rc;
   const size_t notf = (size_t)nx_otf * ny_otf * nz_otf;
@@ -616,6 +679,292 @@ static int init_session(Session& s, int nx, int ny, int nz, float dr, float dz, 
   const int gx = (bSkewedDecon && fabs(deskewAngle) > 0.0) ? (int)s.output_nx : (int)s.deskewedXdim;
   if ((rc = ensure_plan(s, gx, s.output_ny, s.output_nz))) return rc;
   s.inited = true;
+  return 0;
+}
+
+// ---------------------------------------------------------------- batch
+// Independent stacks (timepoints, channels, tiles) of any shapes, each with
+// its own OTF.  Per stack: plans, OTF table and work buffers, kept across
+// calls.  The iterations of all stacks are captured once into a CUDA graph:
+// the stacks are sorted by size and dealt round-robin onto kBatchStreams
+// streams forked from the origin stream, so the graph holds that many
+// independent chains and small stacks run concurrently.
+constexpr int kBatchStreams = 8;
+
+struct BatchStack {
+  int nx = 0, ny = 0, nz = 0;  // caller's stack
+  int gx = 0, gy = 0, gz = 0;  // decon grid
+  int otf_w = 0, otf_h = 0;
+  float dr = 0, dz = 0, dr_psf = 0, dz_psf = 0;
+  OtfSpec os;
+  GridPlan plan;
+  DevBuf<float2> raw_otf;
+  DevBuf<float> Xa, Xb, G, raw;
+  DevBuf<float2> S;
+  DevBuf<double> partials;
+  DevBuf<unsigned> counter;
+  DevBuf<float> lam;
+  float* final_x = nullptr;
+  void release() {
+    plan.release();
+    raw_otf.release();
+    Xa.release();
+    Xb.release();
+    G.release();
+    raw.release();
+    S.release();
+    partials.release();
+    counter.release();
+    lam.release();
+  }
+};
+
+struct Batch {
+  std::vector<BatchStack> st;
+  cudaStream_t origin = nullptr;
+  cudaStream_t fan[kBatchStreams] = {};
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_fork = nullptr;
+  cudaEvent_t ev_join[kBatchStreams] = {};
+  cudaGraphExec_t exec = nullptr;
+  int graph_iters = -1;
+  long long graph_launches = 0;
+  long long last_launches = 0;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    graph_iters = -1;
+  }
+  void release() {
+    drop_graph();
+    for (auto& b : st) b.release();
+    st.clear();
+    for (int i = 0; i < kBatchStreams; ++i) {
+      if (fan[i]) cudaStreamDestroy(fan[i]);
+      if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+      fan[i] = nullptr;
+      ev_join[i] = nullptr;
+    }
+    if (origin) cudaStreamDestroy(origin);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    origin = nullptr;
+    ev_in = ev_out = ev_fork = nullptr;
+  }
+};
+static Batch g_b;
+
+static int batch_streams(Batch& b) {
+  if (b.origin) return 0;
+  CDX_CHECK(cudaStreamCreateWithFlags(&b.origin, cudaStreamNonBlocking));
+  CDX_CHECK(cudaEventCreateWithFlags(&b.ev_in, cudaEventDisableTiming));
+  CDX_CHECK(cudaEventCreateWithFlags(&b.ev_out, cudaEventDisableTiming));
+  CDX_CHECK(cudaEventCreateWithFlags(&b.ev_fork, cudaEventDisableTiming));
+  for (int i = 0; i < kBatchStreams; ++i) {
+    CDX_CHECK(cudaStreamCreateWithFlags(&b.fan[i], cudaStreamNonBlocking));
+    CDX_CHECK(cudaEventCreateWithFlags(&b.ev_join[i], cudaEventDisableTiming));
+  }
+  return 0;
+}
+
+// (Re)build the state of one stack for the caller's description; *changed
+// tells whether its shape-dependent state (and so the graph) changed.
+static int batch_setup_stack(BatchStack& b, const cdx_batch_stack& d, bool* changed) {
+  *changed = true;
+  if (d.nx < 2 || d.ny < 2 || d.nz < 2) {
+    set_error("cdx_RL_batch_device", "stack sizes must be at least 2");
+    return cudaErrorInvalidValue;
+  }
+  const int gx = (int)find_optimal_dimension(d.nx), gy = (int)find_optimal_dimension(d.ny),
+            gz = (int)find_optimal_dimension(d.nz);
+  const bool same = b.plan.valid && b.nx == d.nx && b.ny == d.ny && b.nz == d.nz &&
+                    b.otf_w == d.otf_w && b.otf_h == d.otf_h && b.dr == d.dr && b.dz == d.dz &&
+                    b.dr_psf == d.dr_psf && b.dz_psf == d.dz_psf;
+  *changed = !same;
+  if (same) return 0;
+  b.release();
+  if (gx < 2 || gy < 2 || gz < 2) {
+    set_error("cdx_RL_batch_device", "no FFT-friendly size below the stack size");
+    return cudaErrorInvalidValue;
+  }
+  if (d.otf_w < 2 || d.otf_h < 2 || (d.otf_w & 1) ||
+      !otf_spec_dims(d.otf_w, d.otf_h, 1, d.dr_psf, d.dz_psf, b.os)) {
+    set_error("cdx_RL_batch_device", "OTF table too small or of odd width");
+    return cudaErrorInvalidValue;
+  }
+  b.nx = d.nx;
+  b.ny = d.ny;
+  b.nz = d.nz;
+  b.gx = gx;
+  b.gy = gy;
+  b.gz = gz;
+  b.otf_w = d.otf_w;
+  b.otf_h = d.otf_h;
+  b.dr = d.dr;
+  b.dz = d.dz;
+  b.dr_psf = d.dr_psf;
+  b.dz_psf = d.dz_psf;
+  const size_t n = (size_t)gx * gy * gz;
+  const Geom g = make_geom(gx, gy, gz);
+  int rc;
+  if ((rc = b.raw_otf.ensure((size_t)d.otf_w * d.otf_h / 2)) || (rc = b.Xa.ensure(n)) ||
+      (rc = b.Xb.ensure(n)) || (rc = b.G.ensure(n)) || (rc = b.raw.ensure(n)) ||
+      (rc = b.S.ensure((size_t)g.spec_elems())) ||
+      (rc = b.partials.ensure(2 * (size_t)x_pass_blocks(g))) || (rc = b.counter.ensure(1)) ||
+      (rc = b.lam.ensure(2)))
+    return rc;
+  b.os.raw_otf = b.raw_otf.p;
+  return 0;
+}
+
+// Capture the iterations of every stack into b.exec.
+static int batch_capture(Batch& b, int nIters) {
+  b.drop_graph();
+  std::vector<int> order(b.st.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  std::sort(order.begin(), order.end(), [&](int a, int c) {
+    return (long long)b.st[a].gx * b.st[a].gy * b.st[a].gz >
+           (long long)b.st[c].gx * b.st[c].gy * b.st[c].gz;
+  });
+  const int K = std::min<int>(kBatchStreams, (int)b.st.size());
+  CDX_CHECK(cudaStreamBeginCapture(b.origin, cudaStreamCaptureModeRelaxed));
+  int rc = 0;
+  long long launches = 0;
+  cudaError_t e = cudaEventRecord(b.ev_fork, b.origin);
+  for (int k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b.fan[k], b.ev_fork, 0);
+  if (e != cudaSuccess) {
+    set_cuda_error("batch capture", e);
+    rc = e;
+  }
+  for (size_t j = 0; j < order.size() && !rc; ++j) {
+    BatchStack& t = b.st[order[j]];
+    cudaStream_t s = b.fan[j % K];
+    const size_t n = (size_t)t.gx * t.gy * t.gz;
+    if ((e = cudaMemsetAsync(t.counter.p, 0, sizeof(unsigned), s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(t.lam.p, 0, 2 * sizeof(float), s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(t.raw.p, t.Xa.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess) {
+      set_cuda_error("batch capture", e);
+      rc = e;
+      break;
+    }
+    const LoopBufs lb{t.Xa.p, t.Xb.p, t.G.p, t.raw.p, t.S.p, t.partials.p, t.counter.p, t.lam.p,
+                      (int)(t.partials.n / 2)};
+    rc = rl_loop(t.plan, lb, nIters, s, false, &t.final_x, &launches);
+  }
+  for (int k = 0; k < K && !rc; ++k) {
+    if ((e = cudaEventRecord(b.ev_join[k], b.fan[k])) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(b.origin, b.ev_join[k], 0)) != cudaSuccess) {
+      set_cuda_error("batch capture", e);
+      rc = e;
+    }
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(b.origin, &graph);
+  if (!rc && e != cudaSuccess) {
+    set_cuda_error("batch capture", e);
+    rc = e;
+  }
+  if (!rc) {
+    e = cudaGraphInstantiate(&b.exec, graph, 0);
+    if (e != cudaSuccess) {
+      set_cuda_error("cudaGraphInstantiate", e);
+      b.exec = nullptr;
+      rc = e;
+    }
+  }
+  if (graph) cudaGraphDestroy(graph);
+  if (rc) {
+    cudaGetLastError();
+    return rc;
+  }
+  b.graph_iters = nIters;
+  b.graph_launches = launches;
+  return 0;
+}
+
+static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStream_t caller) {
+  Batch& b = g_b;
+  if (!stacks || n < 1 || nIters < 0) {
+    set_error("cdx_RL_batch_device", "need at least one stack and nIters >= 0");
+    return cudaErrorInvalidValue;
+  }
+  for (int i = 0; i < n; ++i) {
+    const cdx_batch_stack& d = stacks[i];
+    if (!d.raw || !d.result || !d.otf) {
+      set_error("cdx_RL_batch_device", "null raw, result or otf pointer");
+      return cudaErrorInvalidValue;
+    }
+    if (d.nx < 2 || d.ny < 2 || d.nz < 2) {
+      set_error("cdx_RL_batch_device", "stack sizes must be at least 2");
+      return cudaErrorInvalidValue;
+    }
+    if (d.otf_w < 2 || d.otf_h < 2 || (d.otf_w & 1)) {
+      set_error("cdx_RL_batch_device", "OTF table too small or of odd width");
+      return cudaErrorInvalidValue;
+    }
+    if (!(d.dr > 0.f) || !(d.dz > 0.f) || !(d.dr_psf > 0.f) || !(d.dz_psf > 0.f)) {
+      set_error("cdx_RL_batch_device", "pixel sizes must be positive");
+      return cudaErrorInvalidValue;
+    }
+  }
+  int rc;
+  if ((rc = batch_streams(b))) return rc;
+  bool changed = (int)b.st.size() != n;
+  if (changed) {
+    b.drop_graph();
+    for (auto& t : b.st) t.release();
+    b.st.clear();
+    b.st.resize(n);
+  }
+  for (int i = 0; i < n; ++i) {
+    bool c = false;
+    if ((rc = batch_setup_stack(b.st[i], stacks[i], &c))) {
+      b.drop_graph();
+      b.st[i].release();
+      return rc;
+    }
+    changed = changed || c;
+  }
+  if (changed) b.drop_graph();
+  // after the caller's queued work: the OTF tables, then the cropped,
+  // background-subtracted stacks (into each stack's first estimate)
+  CDX_CHECK(cudaEventRecord(b.ev_in, caller));
+  CDX_CHECK(cudaStreamWaitEvent(b.origin, b.ev_in, 0));
+  long long launches = 0;
+  for (int i = 0; i < n; ++i) {
+    BatchStack& t = b.st[i];
+    const cdx_batch_stack& d = stacks[i];
+    CDX_CHECK(cudaMemcpyAsync(t.raw_otf.p, d.otf, sizeof(float) * (size_t)d.otf_w * d.otf_h,
+                              cudaMemcpyHostToDevice, b.origin));
+    if (!t.plan.valid) {
+      if ((rc = build_plan(t.plan, t.gx, t.gy, t.gz, t.dr, t.dz, t.os, b.origin))) return rc;
+    } else {
+      if ((rc = fill_otf(t.plan, t.dr, t.dz, t.os, b.origin))) return rc;
+    }
+    if ((rc = launch_u16_to_f32_crop(d.raw, d.nx, d.ny, t.gx, t.gy, t.gz, t.Xa.p, d.background, 1,
+                                     b.origin)))
+      return rc;
+    launches += 2;
+  }
+  if (nIters > 0) {
+    if (!b.exec || b.graph_iters != nIters) {
+      // the plans' tables were built on the origin stream
+      CDX_CHECK(cudaStreamSynchronize(b.origin));
+      if ((rc = batch_capture(b, nIters))) return rc;
+    }
+    CDX_CHECK(cudaGraphLaunch(b.exec, b.origin));
+    launches += b.graph_launches;
+  }
+  for (int i = 0; i < n; ++i) {
+    BatchStack& t = b.st[i];
+    const float* src = nIters > 0 ? t.final_x : t.Xa.p;
+    CDX_CHECK(cudaMemcpyAsync(stacks[i].result, src, sizeof(float) * (size_t)t.gx * t.gy * t.gz,
+                              cudaMemcpyDeviceToDevice, b.origin));
+  }
+  CDX_CHECK(cudaEventRecord(b.ev_out, b.origin));
+  CDX_CHECK(cudaStreamWaitEvent(caller, b.ev_out, 0));
+  b.last_launches = launches;
   return 0;
 }
 
@@ -775,6 +1124,8 @@ void RL_cleanup(void) {
 
 void cuda_reset(void) {
   std::lock_guard<std::mutex> lk(g_mu);
+  if (g_b.origin) cudaStreamSynchronize(g_b.origin);
+  g_b.release();
   release_all(g_s);
   g_s.inited = false;
   g_s.intensity_overall0 = 0.;
@@ -1006,6 +1357,27 @@ int cdx_conv3d_device(const float* in, float* out, int nx, int ny, int nz, int c
              cudaStreamSynchronize(st));
   S.release();
   return ok;
+}
+
+
+int cdx_batch_grid(int nx, int ny, int nz, int* gx, int* gy, int* gz) {
+  if (gx) *gx = nx >= 2 ? (int)find_optimal_dimension(nx) : 0;
+  if (gy) *gy = ny >= 2 ? (int)find_optimal_dimension(ny) : 0;
+  if (gz) *gz = nz >= 2 ? (int)find_optimal_dimension(nz) : 0;
+  return 1;
+}
+
+int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return batch_run(stacks, n, nIters, (cudaStream_t)stream) == 0 ? 1 : 0;
+}
+
+long long cdx_batch_last_launch_count(void) { return g_b.last_launches; }
+
+void cdx_batch_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_b.origin) cudaStreamSynchronize(g_b.origin);
+  g_b.release();
 }
 
 }  // extern "C"

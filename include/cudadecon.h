@@ -185,6 +185,46 @@ int cdx_fft_length_supported(int n);
 int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
                    size_t capacity);
 
+/* ---- Batched deconvolution of independent stacks (extension) ----------
+ * No entry point of the reference corresponds to these: pycudadecon
+ * deconvolves timepoints, channels and tiles one RL_interface call at a
+ * time, re-initialising for every shape or OTF.  One stack of a batch: */
+typedef struct cdx_batch_stack {
+  const unsigned short* raw; /* device: (nz, ny, nx) uint16 stack, x fastest */
+  int nx, ny, nz;
+  float* result;             /* device: (gz, gy, gx) float32 (cdx_batch_grid) */
+  const float* otf;          /* host: OTF table as RL_interface_init reads the file:
+                                otf_h rows of otf_w floats (radial tables: nr rows of
+                                nz_otf complex values, kz fastest) */
+  int otf_w, otf_h;
+  float dr, dz, dr_psf, dz_psf; /* pixel sizes of the stack and of the PSF (um) */
+  float background;
+} cdx_batch_stack;
+
+/* Decon grid of a stack: each size rounded down to a product of 2, 3, 5 and
+ * 7 (findOptimalDimension, RL-Biggs-Andrews.cpp:18-43).  Returns 1. */
+int cdx_batch_grid(int nx, int ny, int nz, int* gx, int* gy, int* gz);
+
+/* Deconvolve n stacks of any shapes, each with its own OTF: every stack is
+ * processed as RL_interface processes a stack initialised without deskew or
+ * rotation (crop to its decon grid, background subtraction, nIters
+ * Biggs-Andrews RL iterations; no rescale, apodize, z-blend or mirrored
+ * stack), and the final estimate is written to result.  The iterations of
+ * all stacks run as one CUDA graph whose per-stack chains are spread over
+ * several streams (small stacks run concurrently); the graph is kept and
+ * replayed while the stack shapes, OTF sizes, pixel sizes and nIters stay
+ * the same.  Work runs after the work already queued on `stream` (a
+ * cudaStream_t, or NULL) and the results are complete when the work queued
+ * on `stream` after this call runs.  Returns 1 on success, 0 on failure
+ * (cdx_last_error()). */
+int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* stream);
+
+/* Number of kernel launches (graph nodes included) of the last batch call. */
+long long cdx_batch_last_launch_count(void);
+
+/* Free the batch state (plans, buffers, streams, graph). */
+void cdx_batch_release(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,9 +18,10 @@ ROOT = Path(__file__).resolve().parents[1]
 def _declared_functions():
     text = (ROOT / "include" / "cudadecon.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z_0-9]*\s*\*?\s*([A-Za-z_][A-Za-z_0-9]*)\s*\(",
-                       text, flags=re.M)
-    return sorted(set(n for n in names if n not in ("defined",)))
+    # prototypes: a name, a parameter list (default-argument macros nest one
+    # level of parentheses) and a semicolon
+    names = re.findall(r"([A-Za-z_]\w*)\s*\((?:[^;{}()]|\([^()]*\))*\)\s*;", text)
+    return sorted(set(names))
 
 
 def test_header_declares_reference_abi():
@@ -35,6 +36,35 @@ def test_library_exports_every_declared_symbol(cdx):
     L = cdx.lib()
     missing = [n for n in _declared_functions() if not hasattr(L, n)]
     assert not missing, missing
+
+
+def test_declared_function_count():
+    names = _declared_functions()
+    assert "RL_interface" in names and "cdx_batch_last_launch_count" in names
+    assert len(names) >= 33
+
+
+def test_batch_stack_layout_matches_header(cdx, tmp_path):
+    """The ctypes mirror of struct cdx_batch_stack has the C layout."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in cdx.BatchStack._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include <stdbool.h>\n"
+                   f'#include "{ROOT / "include" / "cudadecon.h"}"\n'
+                   "int main(void) {\n"
+                   '  printf("%zu\\n", sizeof(cdx_batch_stack));\n' +
+                   "".join(f'  printf("%zu\\n", offsetof(cdx_batch_stack, {f}));\n' for f in fields) +
+                   "  return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = [ctypes.sizeof(cdx.BatchStack)] + [getattr(cdx.BatchStack, f).offset for f in fields]
+    assert got == want
 
 
 def test_version_string(cdx):
