@@ -114,7 +114,21 @@ void fft_len_free(FftLen& f) {
   f.has_static = false;
 }
 
-int x_pass_blocks(const Geom& g) { return ceil_div(g.ny, 2 * x_pairs(g.nx)) * g.nz; }
+// Row pairs per block of the x passes: the registered tile of a compile-time
+// plan, else the generic tile.
+static int x_tile_pairs(int nx) {
+  switch (nx) {
+#define CDX_PAIRS_CASE(L, PP) \
+  case L:                     \
+    return PP;
+    CDX_X_PLANS(CDX_PAIRS_CASE)
+#undef CDX_PAIRS_CASE
+    default:
+      return x_pairs(nx);
+  }
+}
+
+int x_pass_blocks(const Geom& g) { return ceil_div(g.ny, 2 * x_tile_pairs(g.nx)) * g.nz; }
 
 __global__ void k_spec_to_std(Geom g, const float2* __restrict__ S, float2* __restrict__ out) {
   const long long n = (long long)g.nz * g.ny * g.nxh;

@@ -7,8 +7,10 @@
 // block has one thread per butterfly of the widest stage, so each thread
 // holds exactly one butterfly per stage.  The twiddle layout is the same as
 // the generic engine's (stage s at offset Ns-1, [r-1][k]), built on the host
-// for the plan's radices.  Lengths that split into two radices (756 = 28*27,
-// 100 = 10*10, 256 = 16*16, 1024 = 32*32) need one shared-memory round trip.
+// for the plan's radices.  Lengths that split into two radices (100 = 10*10,
+// 256 = 16*16, 1024 = 32*32) need one shared-memory round trip; three radices
+// (756 = 9*12*7) cost a second round trip but hold fewer registers per thread
+// and let a block own fewer rows.
 #pragma once
 
 #include "dft_static.cuh"
@@ -49,7 +51,7 @@ constexpr int splan_threads() {
 
 // One stage: radix Q, span NS.  Thread b owns butterfly b (if b < V*L/Q).
 template <int L, int Q, int NS, bool INV, int V, bool VFAST, bool SYNC_MID, bool SYNC_END, class Ld,
-          class St>
+          class St, bool GTW = false>
 __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St& st) {
   constexpr int LR = L / Q;
   constexpr int nbf = V * LR;
@@ -75,7 +77,7 @@ __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St
       const float2* tw = stw + (NS - 1) + k;
 #pragma unroll
       for (int r = 1; r < Q; ++r) {
-        const float2 w = tw[(r - 1) * NS];
+        const float2 w = GTW ? __ldg(tw + (r - 1) * NS) : tw[(r - 1) * NS];
         x[r] = INV ? cmulconj(x[r], w) : cmul(x[r], w);
       }
     }
@@ -232,20 +234,24 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const 
                                          const StL& stL) {
   constexpr int L = Plan::kL;
   constexpr int N = Plan::kN;
-  static_assert(!GTW || (N == 2 && !VFAST), "global twiddles: two-radix row plans only");
+  static_assert(!GTW || !VFAST, "global twiddles: row plans only");
   if constexpr (N == 2 && !VFAST) {
     sfft2_rows<Plan, INV, V, GTW>(stw, io.sm, ld0, stL);
   } else if constexpr (N == 2) {
     sfft2_cols<Plan, INV, V>(stw, io.sm, ld0, stL);
   } else if constexpr (N == 1) {
-    sstage<L, Plan::q(0), 1, INV, V, VFAST, true, StL::kSmem>(stw, ld0, stL);
+    sstage<L, Plan::q(0), 1, INV, V, VFAST, true, StL::kSmem, Ld0, StL, GTW>(stw, ld0, stL);
   } else {
-    sstage<L, Plan::q(0), 1, INV, V, VFAST, Ld0::kSmem, true>(stw, ld0, io);
+    // three or more radices: the stages between work in place on the
+    // natural-order tile (unit-stride reads; the first stage writes at
+    // stride Q0, conflict-free for odd Q0)
+    sstage<L, Plan::q(0), 1, INV, V, VFAST, Ld0::kSmem, true, Ld0, IO, GTW>(stw, ld0, io);
     static_for<N - 2>([&](auto sc) {
       constexpr int s = decltype(sc)::value + 1;
-      sstage<L, Plan::q(s), Plan::ns(s), INV, V, VFAST, true, true>(stw, io, io);
+      sstage<L, Plan::q(s), Plan::ns(s), INV, V, VFAST, true, true, IO, IO, GTW>(stw, io, io);
     });
-    sstage<L, Plan::q(N - 1), Plan::ns(N - 1), INV, V, VFAST, true, StL::kSmem>(stw, io, stL);
+    sstage<L, Plan::q(N - 1), Plan::ns(N - 1), INV, V, VFAST, true, StL::kSmem, IO, StL, GTW>(
+        stw, io, stL);
   }
 }
 
