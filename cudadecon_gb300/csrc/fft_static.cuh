@@ -44,7 +44,7 @@ struct SPlan {
 
 // Threads a block needs for V vectors: one per butterfly of the widest stage.
 template <class Plan, int V>
-constexpr int splan_threads() {
+__host__ __device__ constexpr int splan_threads() {
   const int t = V * (Plan::kL / Plan::qmin());
   return ((t + 31) / 32) * 32;
 }
@@ -250,8 +250,10 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const 
       constexpr int s = decltype(sc)::value + 1;
       sstage<L, Plan::q(s), Plan::ns(s), INV, V, VFAST, true, true, IO, IO, GTW>(stw, io, io);
     });
-    sstage<L, Plan::q(N - 1), Plan::ns(N - 1), INV, V, VFAST, true, StL::kSmem, IO, StL, GTW>(
-        stw, io, stL);
+    // the last stage's reads and writes need a barrier between them only when
+    // its storer writes shared memory
+    sstage<L, Plan::q(N - 1), Plan::ns(N - 1), INV, V, VFAST, StL::kSmem, StL::kSmem, IO, StL,
+           GTW>(stw, io, stL);
   }
 }
 
@@ -281,6 +283,7 @@ template <class Plan, int V, bool VFAST, bool GTW = false>
 struct StaticRunner {
   static constexpr bool kStatic = true;
   static constexpr int kV = V;
+  using SPlanT = Plan;
   static constexpr bool kGlobalTw = GTW;
   // float2s of a row tile: the middle layout, the natural layout and the
   // staged half spectra (V vectors of L/2+1 float4) share it
