@@ -9,6 +9,38 @@
 
 namespace cdx {
 
+// ---------------------------------------------------------------- launch order
+// The pass kernels of an RL iteration are launched with programmatic stream
+// serialization: a pass's blocks may start (and stage their twiddles) while
+// the previous pass of the stream drains its last wave.  Before touching
+// global data that the previous pass reads or writes, each pass waits here
+// until that pass has completed and its writes are visible.  Launched
+// without the attribute, or after a non-kernel operation, the wait returns
+// at once.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Let the next pass of the stream be scheduled once every block of this one
+// has started (its blocks then take SMs as this pass's last wave retires;
+// they still wait for this pass to complete before touching its data).
+__device__ __forceinline__ void grid_dep_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <class... KArgs, class... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------- helpers
 // Float-float accumulation (Knuth's TwoSum): hi + lo carries the running sum
 // with about 48 significant bits, so a thread's partial sums of float

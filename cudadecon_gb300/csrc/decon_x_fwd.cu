@@ -25,11 +25,13 @@ k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, float* Xm1, const float*
   float* Xm1s = Xs + 2 * P * nx;
   const int nr = min(2 * P, g.ny - y0);
   const long long roff = ((long long)z * g.ny + y0) * nx;
+  load_twiddles(fx, stw);
+  grid_dep_wait();
+  grid_dep_launch();
   prefetch_floats(Xs, X + roff, nr * nx);
   if (predict) prefetch_floats(Xm1s, Xm1 + roff, nr * nx);
   cp_async_commit();
   const float lam = predict ? __ldg(lamp) : 0.f;
-  load_twiddles(fx, stw);
   cp_async_wait_all();
   __syncthreads();
   if (predict) {
@@ -76,7 +78,7 @@ static int x_fwd_go(const Geom& g, const FftDev& f, const float* X, float* Xm1,
   const int region = std::max(x_tile_size(g.nx, P), 2 * P * g.nx);
   size_t smem = sizeof(float2) * ((size_t)x_tile_offset(g.nx) + (size_t)region);
   if (int rc = smem_optin(k_x_fwd<Run>, smem)) return rc;
-  k_x_fwd<Run><<<grid, T, smem, st>>>(g, f, X, Xm1, lam, predict, S, P);
+  CDX_CHECK(launch_pdl(k_x_fwd<Run>, grid, dim3(T), smem, st, g, f, X, Xm1, lam, predict, S, P));
   CDX_LAUNCH_CHECK("k_x_fwd");
   return 0;
 }
@@ -110,9 +112,11 @@ k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S, float* __restrict
   const int z = blockIdx.y;
   const int y0 = blockIdx.x * 2 * P;
   float4* stg = reinterpret_cast<float4*>(io.sm);
+  load_twiddles(fx, stw);
+  grid_dep_wait();
+  grid_dep_launch();
   prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
   cp_async_commit();
-  load_twiddles(fx, stw);
   cp_async_wait_all();
   __syncthreads();
   const PackedSpecLoad ld{stg, g.nxh, nx, min(P, (g.ny - y0 + 1) / 2)};
@@ -126,7 +130,7 @@ static int x_plain_go(const Geom& g, const FftDev& f, const float2* S, float* ou
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   size_t smem = sizeof(float2) * (size_t)x_rows_offset(g.nx, P);
   if (int rc = smem_optin(k_x_inv_plain<Run>, smem)) return rc;
-  k_x_inv_plain<Run><<<grid, T, smem, st>>>(g, f, S, out, P);
+  CDX_CHECK(launch_pdl(k_x_inv_plain<Run>, grid, dim3(T), smem, st, g, f, S, out, P));
   CDX_LAUNCH_CHECK("k_x_inv_plain");
   return 0;
 }

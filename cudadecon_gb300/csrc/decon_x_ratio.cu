@@ -21,10 +21,12 @@ k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __rest
   float4* stg = reinterpret_cast<float4*>(io.sm);
   float* raws = reinterpret_cast<float*>(smem + x_rows_offset(nx, P));
   const int nr = min(2 * P, g.ny - y0);
+  load_twiddles(fx, stw);
+  grid_dep_wait();
+  grid_dep_launch();
   prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
   prefetch_floats(raws, raw + ((long long)z * g.ny + y0) * nx, nr * nx);
   cp_async_commit();
-  load_twiddles(fx, stw);
   cp_async_wait_all();
   __syncthreads();
   const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
@@ -40,7 +42,7 @@ static int x_ratio_go(const Geom& g, const FftDev& f, float2* S, const float* ra
   dim3 grid(ceil_div(g.ny, 2 * P), g.nz);
   size_t smem = sizeof(float2) * ((size_t)x_rows_offset(g.nx, P) + (size_t)P * g.nx);
   if (int rc = smem_optin(k_x_inv_ratio_fwd<Run>, smem)) return rc;
-  k_x_inv_ratio_fwd<Run><<<grid, T, smem, st>>>(g, f, S, raw, eps, P);
+  CDX_CHECK(launch_pdl(k_x_inv_ratio_fwd<Run>, grid, dim3(T), smem, st, g, f, S, raw, eps, P));
   CDX_LAUNCH_CHECK("k_x_inv_ratio_fwd");
   return 0;
 }

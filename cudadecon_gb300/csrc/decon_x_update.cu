@@ -98,11 +98,13 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, 
   float* Gs = Ys + 2 * P * nx;
   const int nr = min(2 * P, g.ny - y0);
   const long long roff = ((long long)z * g.ny + y0) * nx;
+  if (!Run::kGlobalTw) load_twiddles(fx, smem);
+  grid_dep_wait();
+  grid_dep_launch();
   prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
   prefetch_floats(Ys, Y + roff, nr * nx);
   if (dots) prefetch_floats(Gs, G + roff, nr * nx);
   cp_async_commit();
-  if (!Run::kGlobalTw) load_twiddles(fx, smem);
   cp_async_wait_all();
   __syncthreads();
   const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
@@ -153,8 +155,8 @@ static int x_update_go(const Geom& g, const FftDev& f, const float2* S, const fl
   }
   size_t smem = sizeof(float2) * ((size_t)upd_rows_offset<Run>(g.nx, P) + 2 * (size_t)P * g.nx);
   if (int rc = smem_optin(k_x_inv_update<Run>, smem)) return rc;
-  k_x_inv_update<Run><<<grid, T, smem, st>>>(g, f, S, Y, Xout, G, dots, w.partials, w.counter,
-                                             lam_next, eps, P);
+  CDX_CHECK(launch_pdl(k_x_inv_update<Run>, grid, dim3(T), smem, st, g, f, S, Y, Xout, G, dots, w.partials, w.counter,
+                                             lam_next, eps, P));
   CDX_LAUNCH_CHECK("k_x_inv_update");
   return 0;
 }

@@ -12,6 +12,8 @@ k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
   float2* stw = smem;
   const auto io = Run::row_tile(smem + ny, ny);
   load_twiddles(fy, stw);
+  grid_dep_wait();
+  grid_dep_launch();
   __syncthreads();
   const SpecRowIO gio{S, (long long)blockIdx.x * V, (long long)g.nxh * g.nz, g.nyp};
   Run::template run<INV>(fy, V, 1.f, false, stw, io, gio, gio);
@@ -23,7 +25,7 @@ static int y_go(const Geom& g, const FftDev& f, float2* S, int V, int T, cudaStr
   size_t smem = fft_smem(g.ny, (long long)V * g.ny);
   dim3 grid((unsigned)((nrows + V - 1) / V));
   if (int rc = smem_optin(k_y_pass<INV, Run>, smem)) return rc;
-  k_y_pass<INV, Run><<<grid, T, smem, st>>>(g, f, S, V);
+  CDX_CHECK(launch_pdl(k_y_pass<INV, Run>, grid, dim3(T), smem, st, g, f, S, V));
   CDX_LAUNCH_CHECK("k_y_pass");
   return 0;
 }

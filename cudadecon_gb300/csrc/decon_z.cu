@@ -56,6 +56,9 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     const auto io = Run::col_tile(smem + (nz + (nz & 1)), W);
     constexpr int kChunks = Run::kV / 2;  // 16-byte chunks per z row
     const float2* src = S + (long long)kx * g.plane + y0;
+    load_twiddles(fz, stw);
+    grid_dep_wait();
+    grid_dep_launch();
     for (int idx = threadIdx.x; idx < nz * kChunks; idx += blockDim.x) {
       const int z = idx / kChunks;
       const int c = idx - z * kChunks;
@@ -86,7 +89,6 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
         valid = 1;
       }
     }
-    load_twiddles(fz, stw);
     cp_async_wait_all();
     __syncthreads();
     if (fwd_only) {
@@ -100,6 +102,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     const SmemIO io{smem + nz, W, 1};
     float2* otf_tile = smem + nz + spad_size(W * nz);
     load_twiddles(fz, stw);
+    grid_dep_wait();
+    grid_dep_launch();
     if (fwd_only) {
       __syncthreads();
       Run::template run<false>(fz, W, invW, true, stw, io, gio, gio);
@@ -149,7 +153,8 @@ static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bo
                     ? sizeof(float2) * ((size_t)(g.nz + (g.nz & 1)) + (size_t)W * g.nz)
                     : fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
   if (int rc = smem_optin(k_z_pass<Run>, smem)) return rc;
-  k_z_pass<Run><<<grid, T, smem, st>>>(g, f, S, otf, conj ? 1 : 0, fwd_only ? 1 : 0, W);
+  CDX_CHECK(launch_pdl(k_z_pass<Run>, grid, dim3(T), smem, st, g, f, S, otf, conj ? 1 : 0,
+                       fwd_only ? 1 : 0, W));
   CDX_LAUNCH_CHECK("k_z_pass");
   return 0;
 }
