@@ -77,7 +77,7 @@ struct UpdateStore {
 };
 
 template <class Run>
-__global__ void __launch_bounds__(kMaxThreads, 1)
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<5>())
 k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, float* Xout,
                float* G, int dots, double* partials, unsigned* counter, float* lam_next,
                float eps, int Pa) {

@@ -34,6 +34,11 @@ struct SPlan {
     for (int i = 1; i < kN; ++i) m = kQ[i] < m ? kQ[i] : m;
     return m;
   }
+  __host__ __device__ static constexpr int qmax() {
+    int m = kQ[0];
+    for (int i = 1; i < kN; ++i) m = kQ[i] > m ? kQ[i] : m;
+    return m;
+  }
   __host__ __device__ static constexpr int prod() {
     int p = 1;
     for (int i = 0; i < kN; ++i) p *= kQ[i];
@@ -263,6 +268,9 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const 
 struct GenericRunner {
   static constexpr bool kStatic = false;
   static constexpr int kV = 0;  // vectors per tile: runtime
+  static constexpr int kThreads = kMaxThreads;  // most threads a block is launched with
+  template <int TARGET>
+  static constexpr int min_blocks() { return 1; }
   static constexpr bool kGlobalTw = false;
   static constexpr int kTileF2 = 0;  // tile size: from the runtime geometry
   using Tile = SmemIO;
@@ -283,6 +291,16 @@ template <class Plan, int V, bool VFAST, bool GTW = false>
 struct StaticRunner {
   static constexpr bool kStatic = true;
   static constexpr int kV = V;
+  static constexpr int kThreads = splan_threads<Plan, V>();
+  // Blocks per SM to ask the compiler to fit (launch bounds): TARGET, lowered
+  // so that each thread keeps about 2*qmax + 28 registers (the radix's values
+  // plus addresses and twiddles) and does not spill.
+  template <int TARGET>
+  static constexpr int min_blocks() {
+    const int fit = 65536 / (kThreads * (2 * Plan::qmax() + 28));
+    const int b = TARGET < fit ? TARGET : fit;
+    return b < 1 ? 1 : b;
+  }
   using SPlanT = Plan;
   static constexpr bool kGlobalTw = GTW;
   // float2s of a row tile: the middle layout, the natural layout and the
