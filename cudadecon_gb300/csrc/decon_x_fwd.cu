@@ -8,7 +8,7 @@ namespace cdx {
 
 // ---------------------------------------------------------------- x forward
 template <class Run>
-__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<5>())
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<6>())
 k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, float* Xm1, const float* __restrict__ lamp,
         int predict, float2* __restrict__ S, int Pa) {
   const int P = tile_vectors<Run>(Pa);

@@ -6,7 +6,7 @@ namespace cdx {
 
 // ---------------------------------------------------------------- x inverse
 template <class Run>
-__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<5>())
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<6>())
 k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __restrict__ raw,
                   float eps, int Pa) {
   const int P = tile_vectors<Run>(Pa);

@@ -297,7 +297,7 @@ struct StaticRunner {
   // plus addresses and twiddles) and does not spill.
   template <int TARGET>
   static constexpr int min_blocks() {
-    const int fit = 65536 / (kThreads * (2 * Plan::qmax() + 28));
+    const int fit = 65536 / (kThreads * (2 * Plan::qmax() + 22));
     const int b = TARGET < fit ? TARGET : fit;
     return b < 1 ? 1 : b;
   }
