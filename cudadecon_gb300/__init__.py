@@ -112,6 +112,12 @@ def _bind(L) -> None:
                                             c_void_p]),
         "cdx_load_image": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), POINTER(c_int), _F,
                                    c_size_t]),
+        "makeOTF": (c_int, [c_char_p, c_char_p, c_int, c_float, c_int, c_bool, c_float, c_float,
+                            c_float, c_float, c_int, c_bool, c_bool]),
+        "cdx_make_otf": (c_int, [_F, c_int, c_int, c_int, c_int, c_float, c_int, c_int, c_float,
+                                 c_float, c_float, c_float, c_int, c_int, c_int, _F, c_size_t,
+                                 POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
+        "cdx_save_image": (c_int, [c_char_p, c_int, c_int, c_int, _F]),
         "cdx_batch_grid": (c_int, [c_int, c_int, c_int, POINTER(c_int), POINTER(c_int),
                                    POINTER(c_int)]),
         "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
@@ -202,6 +208,52 @@ def rl_decon(raw: np.ndarray, background=100.0, n_iters=10, rescale=False, save_
 
 def rl_cleanup() -> None:
     lib().RL_cleanup()
+
+
+# ---------------------------------------------------------------- OTF generation
+_OTF_DEFAULTS = dict(lambdanm=520, dz=0.102, interpkr=10, background=None, NA=1.25, NIMM=1.3,
+                     dr=0.102, krmax=0, cleanup=False, otf_3d=False)
+
+
+def make_otf_file(psf_file, otf_file, **kw) -> None:
+    """makeOTF: PSF file -> OTF file (the reference's libradialft entry point).
+    background=None estimates it from the stack as the reference does."""
+    a = dict(_OTF_DEFAULTS, **kw)
+    rc = lib().makeOTF(str(psf_file).encode(), str(otf_file).encode(), int(a["lambdanm"]),
+                       float(a["dz"]), int(a["interpkr"]), a["background"] is not None,
+                       float(a["background"] or 0.0), float(a["NA"]), float(a["NIMM"]),
+                       float(a["dr"]), int(a["krmax"]), bool(a["cleanup"]), bool(a["otf_3d"]))
+    if rc != 0:
+        _err("makeOTF")
+
+
+def make_otf(psf: np.ndarray, **kw) -> np.ndarray:
+    """cdx_make_otf on a (nz, ny, nx) PSF array.  Returns the OTF image as
+    makeOTF writes it: (nx/2+1, 2*nz) float32 for the radial table (view it
+    as complex64 for the (kr, kz) table), (nz, ny, 2*(nx/2+1)) for the 3D OTF."""
+    a = dict(_OTF_DEFAULTS, **kw)
+    p = np.ascontiguousarray(psf, dtype=np.float32)
+    nz, ny, nx = p.shape
+    L = lib()
+    w, h, d = c_int(0), c_int(0), c_int(0)
+    args = [int(a["lambdanm"]), float(a["dz"]), int(a["interpkr"]), int(a["background"] is not None),
+            float(a["background"] or 0.0), float(a["NA"]), float(a["NIMM"]), float(a["dr"]),
+            int(a["krmax"]), int(bool(a["cleanup"])), int(bool(a["otf_3d"]))]
+    out = np.zeros((nz, ny, 2 * (nx // 2 + 1)) if a["otf_3d"] else (nx // 2 + 1, 2 * nz),
+                   dtype=np.float32)
+    ok = L.cdx_make_otf(_fptr(p), nx, ny, nz, *args, _fptr(out), out.size, ctypes.byref(w),
+                        ctypes.byref(h), ctypes.byref(d))
+    if ok != 1:
+        _err("cdx_make_otf")
+    return out
+
+
+def save_image(path, img: np.ndarray) -> None:
+    """cdx_save_image: write a float32 image ((depth,) height, width) as TIFF."""
+    a = np.ascontiguousarray(img, dtype=np.float32)
+    d, h, w = (1,) * (3 - a.ndim) + a.shape
+    if lib().cdx_save_image(str(path).encode(), w, h, d, _fptr(a)) != 1:
+        _err("cdx_save_image")
 
 
 def batch_grid(shape_zyx):

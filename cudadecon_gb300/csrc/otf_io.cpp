@@ -312,4 +312,83 @@ bool load_image_file(const char* path, HostImage& img, std::string& err) {
   return load_cimg(path, img, err);
 }
 
+
+// Write img as a little-endian, uncompressed float32 TIFF: one page per z
+// slice, each page one strip of width x height samples (the layout radialft
+// writes through libtiff, src/radialft_interface.cpp:194).
+bool save_float_tiff(const char* path, const HostImage& img, std::string& err) {
+  if (img.w < 1 || img.h < 1 || img.d < 1 ||
+      img.data.size() != (size_t)img.w * img.h * img.d) {
+    err = "inconsistent image sizes";
+    return false;
+  }
+  const size_t page = (size_t)img.w * img.h * sizeof(float);
+  const unsigned kEntries = 10;
+  const size_t ifd_size = 2 + kEntries * 12 + 4;
+  std::vector<unsigned char> out;
+  auto put16 = [&](size_t o, unsigned v) {
+    out[o] = v & 255;
+    out[o + 1] = (v >> 8) & 255;
+  };
+  auto put32 = [&](size_t o, unsigned long long v) {
+    for (int b = 0; b < 4; ++b) out[o + b] = (v >> (8 * b)) & 255;
+  };
+  // header, then per page: IFD, then the samples
+  size_t total = 8;
+  for (int z = 0; z < img.d; ++z) total += ifd_size + page;
+  if (total > 0xFFFFFFFFull) {
+    err = "image too large for a classic TIFF";
+    return false;
+  }
+  out.assign(total, 0);
+  out[0] = 'I';
+  out[1] = 'I';
+  put16(2, 42);
+  size_t pos = 8;
+  put32(4, pos);
+  for (int z = 0; z < img.d; ++z) {
+    const size_t ifd = pos, data = ifd + ifd_size;
+    const size_t next = (z + 1 < img.d) ? data + page : 0;
+    put16(ifd, kEntries);
+    size_t e = ifd + 2;
+    auto entry = [&](unsigned tag, unsigned type, unsigned long long count, unsigned long long v) {
+      put16(e, tag);
+      put16(e + 2, type);
+      put32(e + 4, count);
+      if (type == 3 && count == 1) put16(e + 8, (unsigned)v);
+      else put32(e + 8, v);
+      e += 12;
+    };
+    entry(256, 4, 1, (unsigned)img.w);   // ImageWidth
+    entry(257, 4, 1, (unsigned)img.h);   // ImageLength
+    entry(258, 3, 1, 32);                // BitsPerSample
+    entry(259, 3, 1, 1);                 // Compression: none
+    entry(262, 3, 1, 1);                 // Photometric: min-is-black
+    entry(273, 4, 1, data);              // StripOffsets
+    entry(277, 3, 1, 1);                 // SamplesPerPixel
+    entry(278, 4, 1, (unsigned)img.h);   // RowsPerStrip
+    entry(279, 4, 1, page);              // StripByteCounts
+    entry(339, 3, 1, 3);                 // SampleFormat: IEEE float
+    put32(e, next);
+    const float* src = img.data.data() + (size_t)z * img.w * img.h;
+    for (size_t i = 0; i < (size_t)img.w * img.h; ++i) {
+      unsigned u;
+      memcpy(&u, src + i, 4);
+      put32(data + 4 * i, u);
+    }
+    pos = data + page;
+  }
+  FILE* f = fopen(path, "wb");
+  if (!f) {
+    err = "cannot open output file";
+    return false;
+  }
+  const bool ok = fwrite(out.data(), 1, out.size(), f) == out.size();
+  if (fclose(f) != 0 || !ok) {
+    err = "write failed";
+    return false;
+  }
+  return true;
+}
+
 }  // namespace cdx

@@ -12,5 +12,7 @@ struct HostImage {
 };
 
 bool load_image_file(const char* path, HostImage& img, std::string& err);
+// Little-endian uncompressed float32 TIFF, one page per z slice.
+bool save_float_tiff(const char* path, const HostImage& img, std::string& err);
 
 }  // namespace cdx

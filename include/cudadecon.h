@@ -185,6 +185,36 @@ int cdx_fft_length_supported(int n);
 int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
                    size_t capacity);
 
+/* ---- OTF generation ---------------------------------------------------
+ * makeOTF of the reference's libradialft (src/radialft_interface.cpp:52-58,
+ * 95-197): reads a PSF stack (TIFF or .cimg), finds the bead (peak and
+ * parabola fits) and the background, subtracts it, and writes the
+ * radially averaged OTF RL_interface_init reads (float32 TIFF of width
+ * 2*nz and height nx/2+1, complex, kz fastest) or, with b3Dout, the 3D OTF
+ * (width 2*(nx/2+1), height ny, depth nz).  The transform runs on the GPU
+ * with this library's FFT, so each PSF size must be a product of 2, 3, 5
+ * and 7 (the reference uses FFTW, which takes any size).  Returns 0 on
+ * success and 1 on failure, as the reference does (cdx_last_error()). */
+int makeOTF(const char* const ifiles, const char* const ofiles, int lambdanm CDX_DEFAULT(520),
+            float dz CDX_DEFAULT(0.102f), int interpkr CDX_DEFAULT(10),
+            bool bUserBackground CDX_DEFAULT(false), float background CDX_DEFAULT(90),
+            float NA CDX_DEFAULT(1.25f), float NIMM CDX_DEFAULT(1.3f), float dr CDX_DEFAULT(0.102f),
+            int krmax CDX_DEFAULT(0), bool bDoCleanup CDX_DEFAULT(false),
+            bool b3Dout CDX_DEFAULT(false));
+
+/* makeOTF on a PSF in host memory ((nz, ny, nx) float32, x fastest), with the
+ * OTF image returned in `out` (capacity in floats; NULL to query the sizes)
+ * instead of a file.  Returns 1 on success, 0 on failure (extension). */
+int cdx_make_otf(const float* psf, int nx, int ny, int nz, int lambdanm, float dz, int interpkr,
+                 int bUserBackground, float background, float NA, float NIMM, float dr, int krmax,
+                 int bDoCleanup, int b3Dout, float* out, size_t capacity, int* out_w, int* out_h,
+                 int* out_d);
+
+/* Write a float32 image (width x height x depth, x fastest) as an
+ * uncompressed TIFF, one page per z, e.g. an OTF table for
+ * RL_interface_init.  Returns 1 on success (extension; host only). */
+int cdx_save_image(const char* path, int width, int height, int depth, const float* data);
+
 /* ---- Batched deconvolution of independent stacks (extension) ----------
  * No entry point of the reference corresponds to these: pycudadecon
  * deconvolves timepoints, channels and tiles one RL_interface call at a

@@ -41,6 +41,9 @@ def oracle():
 
 
 def rel_l2(a, b):
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    """||a - b|| / ||b|| in double (complex arrays compared as complex)."""
+    cplx = np.iscomplexobj(a) or np.iscomplexobj(b)
+    dt = np.complex128 if cplx else np.float64
+    a = np.asarray(a, dtype=dt)
+    b = np.asarray(b, dtype=dt)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
