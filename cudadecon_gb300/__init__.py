@@ -118,6 +118,8 @@ def _bind(L) -> None:
                                  c_float, c_float, c_float, c_int, c_int, c_int, _F, c_size_t,
                                  POINTER(c_int), POINTER(c_int), POINTER(c_int)]),
         "cdx_save_image": (c_int, [c_char_p, c_int, c_int, c_int, _F]),
+        "cdx_wiener_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
+                                      c_float, c_float, c_void_p]),
         "cdx_batch_grid": (c_int, [c_int, c_int, c_int, POINTER(c_int), POINTER(c_int),
                                    POINTER(c_int)]),
         "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
@@ -208,6 +210,23 @@ def rl_decon(raw: np.ndarray, background=100.0, n_iters=10, rescale=False, save_
 
 def rl_cleanup() -> None:
     lib().RL_cleanup()
+
+
+def wiener(stack, background=100.0, wiener=0.01, NA=1.2, wavelength=0.525, stream=None):
+    """cdx_wiener_device on a (nz, ny, nx) float32 CUDA tensor (the decon grid
+    of the last rl_init); returns the filtered CUDA tensor."""
+    import torch
+    x = stack.contiguous().float()
+    nz, ny, nx = x.shape
+    out = torch.empty_like(x)
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    ok = lib().cdx_wiener_device(c_void_p(x.data_ptr()), c_void_p(out.data_ptr()), nx, ny, nz,
+                                 float(background), float(wiener), float(NA), float(wavelength),
+                                 c_void_p(stream.cuda_stream))
+    if ok != 1:
+        _err("cdx_wiener_device")
+    return out
 
 
 # ---------------------------------------------------------------- OTF generation

@@ -1380,4 +1380,55 @@ void cdx_batch_release(void) {
   g_b.release();
 }
 
+
+int cdx_wiener_device(const float* in, float* out, int nx, int ny, int nz, float background,
+                      float wiener, float NA, float wavelength, void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!s.inited || !s.raw_otf.p) {
+    set_error("cdx_wiener_device", "RL_interface_init has not succeeded");
+    return 0;
+  }
+  if (s.od.ny_otf != 1) {
+    set_error("cdx_wiener_device", "the Wiener filter takes a radially averaged OTF");
+    return 0;
+  }
+  if (!(wiener > 0.f) || !(NA > 0.f) || !(wavelength > 0.f) || !in || !out) {
+    set_error("cdx_wiener_device", "wiener, NA and wavelength must be positive");
+    return 0;
+  }
+  if (ensure_stream(s) || ensure_plan(s, nx, ny, nz)) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const GridPlan& p = s.plan;
+  const Geom& g = p.g;
+  // wienerfilter's constants (linearDecon.cpp:898-908, 127-130): k steps of
+  // the grid, their ratio to the OTF's, cutoff 2 NA / lambda
+  const float dkx = 1.0 / (s.dr * nx);
+  const float dky = 1.0 / (s.dr * ny);
+  const float dkz = 1.0 / (s.dz * nz);
+  const float rcutoff = 2 * NA / wavelength;
+  const float w = wiener * wiener;
+  const float kxscale = dkx / s.dkx_otf, kyscale = dky / s.dkx_otf, kzscale = dkz / s.dkz_otf;
+  DevBuf<float2> S, H;
+  DevBuf<float> tmp;
+  OtfDev hd{};
+  int ok = !(S.ensure((size_t)g.spec_elems()) || H.ensure((size_t)g.spec_elems()) ||
+             tmp.ensure((size_t)g.nvox()));
+  if (ok) {
+    hd.mode = 1;
+    hd.full = H.p;
+    ok = !(launch_minus(in, tmp.p, g.nvox(), background, st) ||
+           launch_wiener_h(g, s.raw_otf.p, (int)s.od.nx_otf, (int)s.od.nz_otf, dkx, dky, kxscale,
+                           kyscale, kzscale, rcutoff, w, H.p, st) ||
+           launch_x_fwd(g, p.fx, tmp.p, nullptr, nullptr, 0, S.p, st) ||
+           launch_y_pass(g, p.fy, S.p, false, st) || launch_z_pass(g, p.fz, S.p, hd, false, st) ||
+           launch_y_pass(g, p.fy, S.p, true, st) || launch_x_inv_plain(g, p.fx, S.p, out, st) ||
+           cudaStreamSynchronize(st));
+  }
+  S.release();
+  H.release();
+  tmp.release();
+  return ok;
+}
+
 }  // extern "C"

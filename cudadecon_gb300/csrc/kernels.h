@@ -121,4 +121,12 @@ int launch_f32_to_u16(const float* in, unsigned short* out, long long n, cudaStr
 int affine_host(const float* in, int nx, int ny, int nz, const float* mat16, bool ra, float dx,
                 float dy, float dz, float* out, cudaStream_t st);
 
+// Wiener filter factor conj(OTF)(1 - kr/rcutoff)/(|OTF|^2 + w) / N in the
+// spectrum layout, from the radial OTF table (nr x nzotf complex).
+int launch_wiener_h(const Geom& g, const float2* otf, int nr, int nzotf, float dkx, float dky,
+                    float kxscale, float kyscale, float kzscale, float rcutoff, float w,
+                    float2* H, cudaStream_t st);
+// out = in - bg (no clamp).
+int launch_minus(const float* in, float* out, long long n, float bg, cudaStream_t st);
+
 }  // namespace cdx

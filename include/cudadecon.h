@@ -185,6 +185,16 @@ int cdx_fft_length_supported(int n);
 int cdx_load_image(const char* path, int* width, int* height, int* depth, float* out,
                    size_t capacity);
 
+/* One-step Wiener filter instead of RL (the reference's CLI option --wiener,
+ * linearDecon.cpp:116-168 and 1116-1127; no ABI entry point there): out =
+ * IFFT( FFT(in - background) * conj(OTF) (1 - kr/kc) / (|OTF|^2 + wiener^2) ),
+ * kc = 2 NA / wavelength (1/um), zero beyond kc, with the OTF (a radial
+ * table) and pixel sizes of the last RL_interface_init.  in and out are
+ * device pointers on the (nz, ny, nx) grid (each size a product of 2, 3, 5
+ * and 7).  Returns 1 on success, 0 on failure (extension). */
+int cdx_wiener_device(const float* in, float* out, int nx, int ny, int nz, float background,
+                      float wiener, float NA, float wavelength, void* stream);
+
 /* ---- OTF generation ---------------------------------------------------
  * makeOTF of the reference's libradialft (src/radialft_interface.cpp:52-58,
  * 95-197): reads a PSF stack (TIFF or .cimg), finds the bead (peak and

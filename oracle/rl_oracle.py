@@ -491,3 +491,53 @@ def affine(stack, mat4x4, ra=False, dx=1.0, dy=1.0, dz=1.0):
            az * ((1 - ay) * ((1 - ax) * T(k + 1, j, i) + ax * T(k + 1, j, i + 1)) +
                  ay * ((1 - ax) * T(k + 1, j + 1, i) + ax * T(k + 1, j + 1, i + 1))))
     return out.astype(np.float32)
+
+
+def otfinterpolate(otf, kx, ky, kz):
+    """otfinterpolate (linearDecon.cpp:78-114), vectorised: bilinear
+    interpolation of the radial table otf (nr, nzotf) at the (sub-pixel)
+    OTF coordinates (kx, ky, kz), kz wrapping; 0 outside the table."""
+    nr, nzotf = otf.shape
+    kx, ky, kz = (np.asarray(a, dtype=F32) for a in (kx, ky, kz))
+    krindex = np.sqrt((kx * kx + ky * ky).astype(F32)).astype(F32)
+    kzindex = np.where(kz < 0, (kz + F32(nzotf)).astype(F32), kz)
+    inside = (krindex < nr - 1) & (kzindex < nzotf)
+    ir = np.where(inside, np.floor(krindex), 0).astype(np.int64)
+    iz = np.where(inside, np.floor(kzindex), 0).astype(np.int64)
+    ar = (krindex - ir).astype(np.float64)
+    az = (kzindex - iz).astype(np.float64)
+    iz1 = np.where(iz == nzotf - 1, 0, iz + 1)
+    o = otf.astype(np.complex128)
+    v = (1 - ar) * (o[ir, iz] * (1 - az) + o[ir, iz1] * az) + ar * (o[ir + 1, iz] * (1 - az)
+                                                                  + o[ir + 1, iz1] * az)
+    return np.where(inside, v, 0)
+
+
+def wiener(state: InitState, img, background, wiener_const, NA, wavelength):
+    """One-step Wiener filter of the reference's CLI (wienerfilter,
+    linearDecon.cpp:116-168, applied at 1116-1127) on a float32 (nz, ny, nx)
+    volume on the decon grid, with the OTF and pixel sizes of `state`."""
+    x = np.asarray(img, dtype=F32) - F32(background)
+    nz, ny, nx = x.shape
+    dkx = F32(1.0 / (float(state.dr) * nx))
+    dky = F32(1.0 / (float(state.dr) * ny))
+    dkz = F32(1.0 / (float(state.dz) * nz))
+    kxscale = F32(dkx / state.dkx_otf)
+    kyscale = F32(dky / state.dkx_otf)
+    kzscale = F32(dkz / state.dkz_otf)
+    rcutoff = F32(2 * F32(NA) / F32(wavelength))
+    w = F32(wiener_const) * F32(wiener_const)
+    kz = np.arange(nz)
+    kz = np.where(kz > nz // 2, kz - nz, kz).astype(F32)[:, None, None]
+    ky = np.arange(ny)
+    ky = np.where(ky > ny // 2, ky - ny, ky).astype(F32)[None, :, None]
+    kx = np.arange(nx // 2 + 1).astype(F32)[None, None, :]
+    kr = np.sqrt((kx * kx * dkx * dkx + ky * ky * dky * dky).astype(F32)).astype(F32)
+    kr = np.broadcast_to(kr, (nz, ny, nx // 2 + 1))
+    o = otfinterpolate(state.otf, np.broadcast_to(kx * kxscale, kr.shape),
+                       np.broadcast_to(ky * kyscale, kr.shape), np.broadcast_to(kz * kzscale, kr.shape))
+    amp2 = np.abs(o) ** 2
+    rho = kr.astype(np.float64) / float(rcutoff)
+    H = np.where(kr <= rcutoff, np.conj(o) * (1 - rho) / (amp2 + float(w)), 0)
+    G = np.fft.rfftn(x.astype(np.float64))
+    return np.fft.irfftn(G * H, s=x.shape).astype(np.float32)
