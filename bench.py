@@ -210,6 +210,81 @@ def run_reference(args):
     return 0
 
 
+BATCH = {"stacks": 64, "iterations": 10, "seed": 1003, "z": (32, 160), "y": (128, 512),
+         "x": (128, 1024)}
+
+
+def run_batch(cdx, dev, reps=3):
+    """Config 4: uneven stacks with their own OTFs through cdx_RL_batch_device
+    (one CUDA graph per call), and the same stacks through per-stack calls
+    (RL_interface_init + cdx_RL_device each) for comparison.  Stacks are a
+    Poisson background plus sparse point beads, generated on the GPU (seeded);
+    OTFs are Gaussian with sigmas jittered by +-20%."""
+    import torch
+    from cudadecon_gb300 import synth
+    rng = np.random.default_rng(BATCH["seed"])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(BATCH["seed"])
+    stacks, vox = [], 0
+    for _ in range(BATCH["stacks"]):
+        shape = tuple(int(rng.choice(synth.smooth_sizes(*BATCH[a]))) for a in ("z", "y", "x"))
+        j = rng.uniform(0.8, 1.2, 2)
+        tab = synth.gaussian_otf_table(129, 64, 1.5 * j[0], 4.0 * j[1])
+        lam = 100.0 + 3000.0 * (torch.rand(shape, generator=gen, device=dev) < 2e-4).float()
+        raw = torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.uint16)
+        stacks.append(dict(raw=raw, otf=tab, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.3,
+                           background=100.0))
+        vox += int(np.prod(cdx.batch_grid(shape)))
+    iters = BATCH["iterations"]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    outs = cdx.rl_batch(stacks, n_iters=iters)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    st = torch.cuda.current_stream()
+    e0.record(st)
+    for _ in range(reps):
+        outs = cdx.rl_batch(stacks, n_iters=iters)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    finite = all(bool(torch.isfinite(o).all().item()) for o in outs)
+    launches = int(cdx.lib().cdx_batch_last_launch_count())
+    del outs
+    cdx.lib().cdx_batch_release()
+    # the same stacks one call at a time, as a per-stack caller does
+    L = cdx.lib()
+    with tempfile.TemporaryDirectory() as td:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i, d in enumerate(stacks):
+            p = Path(td) / f"otf{i}.tif"
+            synth.write_otf(p, d["otf"])
+            nz, ny, nx = d["raw"].shape
+            cdx.rl_init((nz, ny, nx), p, dr=d["dr"], dz=d["dz"], dr_psf=d["dr_psf"],
+                        dz_psf=d["dz_psf"], deskew_angle=0.0, rotation_angle=0.0)
+            out = torch.empty(cdx.output_shape(), dtype=torch.float32, device=dev)
+            ok = L.cdx_RL_device(ctypes.c_void_p(d["raw"].data_ptr()), nx, ny, nz,
+                                 ctypes.c_void_p(out.data_ptr()), None, d["background"], False,
+                                 False, iters, 0, 0, 0, 0.0, False, False,
+                                 ctypes.c_void_p(st.cuda_stream))
+            if ok != 1:
+                raise RuntimeError(L.cdx_last_error().decode())
+        torch.cuda.synchronize()
+        seq_s = time.perf_counter() - t0
+    cdx.rl_cleanup()
+    return {"workload": f"{BATCH['stacks']} uneven stacks, z/y/x 2-3-5-7-smooth in "
+                        f"{BATCH['z']}/{BATCH['y']}/{BATCH['x']}, own Gaussian OTF each, "
+                        f"{iters} RL iterations",
+            "decon_voxels": vox, "value": vox * iters / (ms * 1e-3), "unit": "voxel-iter/s",
+            "ms_per_call": ms, "first_call_s": first_s, "graph_launches_per_call": launches,
+            "per_stack_calls_value": vox * iters / seq_s, "per_stack_calls_s": seq_s,
+            "data": "synthetic: Poisson background 100 plus sparse point beads, seeded, on the GPU",
+            "output_finite": finite}
+
+
 def run_gb300(args):
     import torch
     world, rank, local, pg = dist_setup(args)
@@ -347,6 +422,10 @@ def run_gb300(args):
                "sample": f"2 of 15 RL iterations on the deskewed {nvox}-voxel volume "
                          f"(scipy.fft float32, {cores} threads), {dt:.1f} s"}
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = run_batch(cdx, dev)
+
     if rank == 0:
         line = {
             "metric": "RL voxel-iterations/s", "value": value, "unit": "voxel-iter/s",
@@ -371,6 +450,7 @@ def run_gb300(args):
             "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
             "output_finite": finite,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     td.cleanup()
@@ -384,6 +464,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched uneven-stacks measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
