@@ -102,7 +102,7 @@ int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, float* Xm1,
 
 
 template <class Run>
-__global__ void __launch_bounds__(kMaxThreads, 1)
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<6>())
 k_x_inv_plain(Geom g, FftDev fx, const float2* __restrict__ S, float* __restrict__ out, int Pa) {
   const int P = tile_vectors<Run>(Pa);
   extern __shared__ __align__(16) float2 smem[];

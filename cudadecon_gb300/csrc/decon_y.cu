@@ -5,7 +5,7 @@ namespace cdx {
 
 // ---------------------------------------------------------------- y pass
 template <bool INV, class Run>
-__global__ void __launch_bounds__(kMaxThreads, 1)
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<8>())
 k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
   extern __shared__ float2 smem[];
   const int ny = g.ny;

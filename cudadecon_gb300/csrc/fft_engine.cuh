@@ -29,8 +29,8 @@
 namespace cdx {
 
 constexpr int kMaxStages = 14;
-constexpr int kEpt = 16;        // maximum complex elements held per thread per stage
-constexpr int kMaxThreads = 512; // FFT kernels launch at most this many threads
+constexpr int kEpt = 8;         // maximum complex elements held per thread per stage
+constexpr int kMaxThreads = 1024; // FFT kernels launch at most this many threads
 // Longest transform: one vector must fit a tile of kMaxThreads * kEpt elements.
 constexpr int kMaxFftLen = kMaxThreads * kEpt;
 
