@@ -188,11 +188,6 @@ static int make_otf_device(float* d_psf, int nx, int ny, int nz, const OtfMakePa
   int *d_start = nullptr, *d_offs = nullptr;
   FftLen fx, fy, fz;
   const Geom g = make_geom(nx, ny, nz);
-  int rc = 0;
-  auto fail = [&](int code) {
-    rc = code;
-    return code;
-  };
   auto cleanup_all = [&]() {
     cudaFree(d_bmax);
     cudaFree(d_bidx);
@@ -212,7 +207,7 @@ static int make_otf_device(float* d_psf, int nx, int ny, int nz, const OtfMakePa
     if (e_ != cudaSuccess) {            \
       set_cuda_error("makeOTF", e_);    \
       cleanup_all();                    \
-      return fail(e_);                  \
+      return e_;                        \
     }                                   \
   } while (0)
   OTF_CHECK(cudaMalloc(&d_bmax, kRedBlocks * sizeof(float)));
@@ -285,7 +280,7 @@ static int make_otf_device(float* d_psf, int nx, int ny, int nz, const OtfMakePa
   // ---- unnormalised 3D R2C (the reference's fftwf_plan_dft_r2c_3d, 135-142)
   if (fft_len_init(fx, nx) || fft_len_init(fy, ny) || fft_len_init(fz, nz)) {
     cleanup_all();
-    return fail(cudaErrorInvalidValue);
+    return cudaErrorInvalidValue;
   }
   const OtfDev none{};
   OTF_CHECK(cudaMalloc(&d_S, sizeof(float2) * (size_t)g.spec_elems()));
@@ -294,7 +289,7 @@ static int make_otf_device(float* d_psf, int nx, int ny, int nz, const OtfMakePa
       launch_y_pass(g, fy, d_S, false, st) || launch_z_pass(g, fz, d_S, none, false, st, true) ||
       launch_spec_to_std(g, d_S, d_std, st)) {
     cleanup_all();
-    return fail(cudaErrorLaunchFailure);
+    return cudaErrorLaunchFailure;
   }
   // ---- shift_center (286-319)
   const float dphiz = 2 * M_PI * zc / nz;
