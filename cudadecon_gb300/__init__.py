@@ -120,6 +120,9 @@ def _bind(L) -> None:
         "cdx_save_image": (c_int, [c_char_p, c_int, c_int, c_int, _F]),
         "cdx_wiener_device": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_float,
                                       c_float, c_float, c_void_p]),
+        "cdx_RL_tiled": (c_int, [_U16, c_int, c_int, c_int, _F, c_int, c_int, c_int, c_float,
+                                 c_int, c_int, c_int, c_float]),
+        "cdx_mip_device": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
         "cdx_batch_grid": (c_int, [c_int, c_int, c_int, POINTER(c_int), POINTER(c_int),
                                    POINTER(c_int)]),
         "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
@@ -206,6 +209,37 @@ def rl_decon(raw: np.ndarray, background=100.0, n_iters=10, rescale=False, save_
     if ok != 1:
         _err("RL_interface")
     return (out, desk) if save_deskewed else out
+
+
+def rl_tiled(raw: np.ndarray, tile=128, tile_overlap=30, blend=False, background=100.0,
+             n_iters=10, napodize=0, nzblend=0, pad_val=0.0):
+    """cdx_RL_tiled on a (nz, ny, nx) uint16 stack (rl_init must have been
+    called with the tile's ny); returns the stitched float32 result."""
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    nz, ny, nx = raw.shape
+    L = lib()
+    onz, _, onx = output_shape()
+    out = np.zeros((onz, ny if tile else output_shape()[1], onx), dtype=np.float32)
+    ok = L.cdx_RL_tiled(_u16ptr(raw), nx, ny, nz, _fptr(out), int(tile), int(tile_overlap),
+                        int(bool(blend)), float(background), int(n_iters), int(napodize),
+                        int(nzblend), float(pad_val))
+    if ok != 1:
+        _err("cdx_RL_tiled")
+    return out
+
+
+def mip(volume, axis):
+    """cdx_mip_device on a (nz, ny, nx) float32 CUDA tensor; axis 0/1/2 = x/y/z."""
+    import torch
+    v = volume.contiguous().float()
+    nz, ny, nx = v.shape
+    shape = {0: (nz, ny), 1: (nz, nx), 2: (ny, nx)}[axis]
+    out = torch.empty(shape, dtype=torch.float32, device=v.device)
+    ok = lib().cdx_mip_device(c_void_p(v.data_ptr()), nx, ny, nz, int(axis), c_void_p(out.data_ptr()),
+                              c_void_p(torch.cuda.current_stream().cuda_stream))
+    if ok != 1:
+        _err("cdx_mip_device")
+    return out
 
 
 def rl_cleanup() -> None:

@@ -1431,4 +1431,105 @@ int cdx_wiener_device(const float* in, float* out, int nx, int ny, int nz, float
   return ok;
 }
 
+
+int cdx_RL_tiled(const unsigned short* raw, int nx, int ny, int nz, float* result,
+                 int tile_requested, int tile_overlap_requested, int blend, float background,
+                 int nIters, int napodize, int nZblend, float padVal) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!s.inited) {
+    set_error("cdx_RL_tiled", "RL_interface_init has not succeeded");
+    return 0;
+  }
+  if (!raw || !result || nx < 2 || ny < 2 || nz < 2) {
+    set_error("cdx_RL_tiled", "null buffer or sizes below 2");
+    return 0;
+  }
+  // tiling setup of the CLI (linearDecon.cpp:498-519)
+  int tile_size = ny;
+  int ntiles = 1;
+  double overlap = 0;
+  if (tile_requested != 0) {
+    tile_size = tile_requested < 0 ? std::min(128, ny) : std::min(tile_requested, ny);
+    if (tile_size - tile_overlap_requested <= 0) {
+      set_error("cdx_RL_tiled", "tile overlap must be smaller than the tile");
+      return 0;
+    }
+    ntiles = (int)ceil((double)ny / ((double)tile_size - tile_overlap_requested));
+    if (ntiles > 1) overlap = floor(((double)tile_size * ntiles - ny) / (ntiles - 1));
+  }
+  if ((int)s.output_ny != (int)find_optimal_dimension(tile_size) || s.output_nx == 0) {
+    set_error("cdx_RL_tiled", "RL_interface_init must be called with ny = the tile size");
+    return 0;
+  }
+  const int no_zone = (int)ceil((overlap - 4) / 2.0);  // 1175-1245: no zone, blend zone, ...
+  const int blend_zone = (int)(overlap - no_zone - no_zone);
+  RLArgs a{nx, tile_size, nz, background, false, false, nIters, 0, napodize, nZblend, padVal,
+           false, false};
+  if (ensure_stream(s)) return 0;
+  cudaStream_t st = s.stream;
+  const size_t tvox = (size_t)nx * tile_size * nz;
+  DevBuf<unsigned short> d_raw, d_tile;
+  DevBuf<float> stitch;
+  DevBuf<unsigned char> weight;
+  int onx = 0, ony_total = 0, onz = 0;
+  // the raw stack goes to the device once; each tile's rows are gathered there
+  int ok = d_raw.ensure((size_t)nx * ny * nz) == 0 && d_tile.ensure(tvox) == 0 &&
+           cudaMemcpyAsync(d_raw.p, raw, sizeof(unsigned short) * (size_t)nx * ny * nz,
+                           cudaMemcpyHostToDevice, st) == cudaSuccess;
+  if (!ok) set_cuda_error("cdx_RL_tiled", cudaGetLastError());
+  for (int t = 0; ok && t < ntiles; ++t) {
+    const int yoff = (int)floor((double)t * (tile_size - overlap));
+    if (launch_tile_rows(d_raw.p, d_tile.p, nx, ny, nz, tile_size, yoff, st)) {
+      ok = 0;
+      break;
+    }
+    const float* out = nullptr;
+    int dims[3];
+    if (rl_pipeline(s, d_tile.p, a, nullptr, &out, dims)) {
+      ok = 0;
+      break;
+    }
+    if (t == 0) {
+      onx = dims[0];
+      onz = dims[2];
+      ony_total = ntiles > 1 ? ny : dims[1];
+      const size_t n = (size_t)onx * ony_total * onz;
+      if (stitch.ensure(n) || weight.ensure(n) ||
+          cudaMemsetAsync(stitch.p, 0, n * sizeof(float), st) != cudaSuccess ||
+          cudaMemsetAsync(weight.p, 0, n, st) != cudaSuccess) {
+        ok = 0;
+        break;
+      }
+    }
+    if (ntiles == 1) {
+      if (cudaMemcpyAsync(stitch.p, out, sizeof(float) * (size_t)onx * ony_total * onz,
+                          cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        ok = 0;
+    } else if (launch_stitch(out, stitch.p, weight.p, onx, dims[1], onz, ony_total, yoff, overlap,
+                             no_zone, blend_zone, t == 0, t + 1 >= ntiles, blend != 0, st)) {
+      ok = 0;
+    }
+  }
+  if (ok)
+    ok = cudaMemcpyAsync(result, stitch.p, sizeof(float) * (size_t)onx * ony_total * onz,
+                         cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+  else
+    cudaStreamSynchronize(st);
+  d_raw.release();
+  d_tile.release();
+  stitch.release();
+  weight.release();
+  return ok;
+}
+
+int cdx_mip_device(const float* in, int nx, int ny, int nz, int axis, float* out, void* stream) {
+  if (!in || !out || nx < 1 || ny < 1 || nz < 1) {
+    set_error("cdx_mip_device", "null buffer or empty sizes");
+    return 0;
+  }
+  return launch_mip(in, nx, ny, nz, axis, out, (cudaStream_t)stream) == 0 ? 1 : 0;
+}
+
 }  // extern "C"

@@ -129,4 +129,13 @@ int launch_wiener_h(const Geom& g, const float2* otf, int nr, int nzotf, float d
 // out = in - bg (no clamp).
 int launch_minus(const float* in, float* out, long long n, float bg, cudaStream_t st);
 
+// Stitch a deconvolved y tile into the output (the CLI's tiling rules).
+int launch_tile_rows(const unsigned short* raw, unsigned short* tile, int nx, int ny, int nz,
+                     int tny, int yoff, cudaStream_t st);
+int launch_stitch(const float* tile, float* out, unsigned char* weight, int nx, int tny, int nz,
+                  int ny_out, int yoff, double overlap, int no_zone, int blend_zone, bool first,
+                  bool last, bool blend, cudaStream_t st);
+// Maximum-intensity projection along axis 0 (x), 1 (y) or 2 (z).
+int launch_mip(const float* in, int nx, int ny, int nz, int axis, float* out, cudaStream_t st);
+
 }  // namespace cdx

@@ -166,7 +166,7 @@ def bead_stack(shape, n_beads=200, sigma_range=(0.5, 2.0), amp_range=(500.0, 500
             pts = np.concatenate(pts)
             spec += np.fft.rfftn(_splat_points(shape, pts, np.full(len(pts), inten * 0.5)))
     spec *= _gauss_otf_grid(shape, psf_sigma_z, psf_sigma_xy, psf_sigma_xy)
-    img = np.fft.irfftn(spec, s=shape)
+    img = np.fft.irfftn(spec, s=shape, axes=(0, 1, 2))
     img = np.maximum(img, 0) + background
     if poisson:
         img = rng.poisson(img).astype(np.float64)

@@ -195,6 +195,25 @@ int cdx_load_image(const char* path, int* width, int* height, int* depth, float*
 int cdx_wiener_device(const float* in, float* out, int nx, int ny, int nz, float background,
                       float wiener, float NA, float wavelength, void* stream);
 
+/* Y-tiled deconvolution of the CLI (--tile, --TileOverlap, --BlendTileOverlap;
+ * linearDecon.cpp:497-566 and 1175-1245), for stacks whose decon buffers do
+ * not fit the GPU at once: the (nz, ny, nx) u16 host stack is cut into tiles
+ * of tile rows along y (tile < 0: min(128, ny); 0: no tiling) overlapping by
+ * about tile_overlap rows (rows past the stack repeat its last row), each tile
+ * is processed as RL_interface processes a stack (call RL_interface_init with
+ * ny = the tile size first), and the results are stitched back as the CLI
+ * does: each overlap is split between the two tiles, or blended over a few
+ * rows when blend != 0.  result (host) holds get_output_nx() * ny *
+ * get_output_nz() floats.  Returns 1 on success (extension). */
+int cdx_RL_tiled(const unsigned short* raw, int nx, int ny, int nz, float* result, int tile,
+                 int tile_overlap, int blend, float background, int nIters, int napodize,
+                 int nZblend, float padVal);
+
+/* Maximum-intensity projection (the CLI's MIPs, linearDecon.cpp:1434-1473) of a
+ * device (nz, ny, nx) float volume along axis 0 (x; out (nz, ny)), 1 (y; out
+ * (nz, nx)) or 2 (z; out (ny, nx)).  Returns 1 on success (extension). */
+int cdx_mip_device(const float* in, int nx, int ny, int nz, int axis, float* out, void* stream);
+
 /* ---- OTF generation ---------------------------------------------------
  * makeOTF of the reference's libradialft (src/radialft_interface.cpp:52-58,
  * 95-197): reads a PSF stack (TIFF or .cimg), finds the bead (peak and

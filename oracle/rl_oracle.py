@@ -540,4 +540,71 @@ def wiener(state: InitState, img, background, wiener_const, NA, wavelength):
     rho = kr.astype(np.float64) / float(rcutoff)
     H = np.where(kr <= rcutoff, np.conj(o) * (1 - rho) / (amp2 + float(w)), 0)
     G = np.fft.rfftn(x.astype(np.float64))
-    return np.fft.irfftn(G * H, s=x.shape).astype(np.float32)
+    return np.fft.irfftn(G * H, s=x.shape, axes=tuple(range(x.ndim))).astype(np.float32)
+
+
+def tiling(ny, tile_requested, tile_overlap_requested):
+    """Tiling setup of the CLI (linearDecon.cpp:498-519): (tile_size, number
+    of tiles, overlap (double), y offsets)."""
+    if tile_requested == 0:
+        return ny, 1, 0.0, [0]
+    tile = min(128, ny) if tile_requested < 0 else min(tile_requested, ny)
+    n = math.ceil(ny / (tile - tile_overlap_requested))
+    overlap = math.floor((tile * n - ny) / (n - 1)) if n > 1 else 0.0
+    offs = [math.floor(t * (tile - overlap)) for t in range(n)]
+    return tile, n, float(overlap), offs
+
+
+def tile_crop(raw, y0, tile):
+    """Rows y0 .. y0+tile-1 of a (nz, ny, nx) stack; rows past the stack repeat
+    its last row (CImg get_crop with boundary conditions)."""
+    ny = raw.shape[1]
+    idx = np.clip(np.arange(y0, y0 + tile), 0, ny - 1)
+    return np.ascontiguousarray(raw[:, idx, :])
+
+
+def stitch_tiles(tiles, offs, ny_out, overlap, blend_on):
+    """Stitching of the CLI (linearDecon.cpp:1175-1245) of processed tiles
+    (each (nz, tny, nx) float32) at y offsets offs into (nz, ny_out, nx)."""
+    if len(tiles) == 1:
+        return tiles[0].copy()
+    nz, tny, nx = tiles[0].shape
+    out = np.zeros((nz, ny_out, nx), dtype=np.float32)
+    w = np.zeros((nz, ny_out, nx), dtype=bool)
+    no_zone = math.ceil((overlap - 4) / 2.0)
+    blend_zone = int(overlap - no_zone - no_zone)
+    n = len(tiles)
+    for t, (img, yoff) in enumerate(zip(tiles, offs)):
+        first, last = t == 0, t + 1 >= n
+        for y in range(tny):
+            if first and y <= overlap:
+                b = F32(1)
+            elif last and y >= tny - overlap:
+                b = F32(1)
+            elif y <= no_zone:
+                b = F32(0)
+            elif no_zone < y <= no_zone + blend_zone:
+                b = F32((y - no_zone) / blend_zone)
+            elif y >= tny - no_zone:
+                b = F32(0)
+            else:
+                b = F32(1)
+            yo = y + yoff
+            if yo >= ny_out:
+                continue
+            v = img[:, y, :]
+            if blend_on:
+                cur, ww = out[:, yo, :], w[:, yo, :]
+                if 0 < b < 1:
+                    mixed = ((v * b).astype(np.float64) + cur.astype(np.float64) * (1.0 - float(b))).astype(F32)
+                    out[:, yo, :] = np.where(ww, mixed, v)
+                elif b == 1:
+                    out[:, yo, :] = v
+                if b > 0:
+                    w[:, yo, :] = True
+            else:
+                past_front = y >= math.floor(float(F32(overlap)) / 2.0) or first
+                before_end = y < math.floor(tny - float(F32(overlap)) / 2.0) or last
+                if past_front and before_end:
+                    out[:, yo, :] = v
+    return out
