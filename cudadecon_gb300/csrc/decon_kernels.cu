@@ -150,8 +150,10 @@ int launch_spec_to_std(const Geom& g, const float2* S, float2* out, cudaStream_t
 
 // ---------------------------------------------------------------- OTF tables
 // Radially averaged OTF resampled along kz for every z frequency of the
-// volume: tz[ir][z] = otf[ir][iz]*(1-az) + otf[ir][iz+1 (wrapping)]*az, zero
-// where kzindex falls outside [0, nz_otf), times scale (= 1/N).
+// volume: tz[z][ir] = otf[ir][iz]*(1-az) + otf[ir][iz+1 (wrapping)]*az, zero
+// where kzindex falls outside [0, nz_otf), times scale (= 1/N).  The radius
+// runs fastest, so the columns of a z tile (neighbouring ky, hence
+// neighbouring radii) gather from one or two cache lines per kz.
 // Follows dev_otfinterpolate's RA branch (RLgpuImpl.cu:233-273) with the kz
 // coordinate of makeOTFarray_kernel (RLgpuImpl.cu:357).
 __global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2* __restrict__ otf,
@@ -171,7 +173,7 @@ __global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2*
     const float2 b = otf[(long long)ir * nzotf + izp];
     v = make_float2(a.x * (1.f - az) + b.x * az, a.y * (1.f - az) + b.y * az);
   }
-  tz[(long long)ir * nz + z] = make_float2(v.x * scale, v.y * scale);
+  tz[(long long)z * nr + ir] = make_float2(v.x * scale, v.y * scale);
 }
 
 int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* tz,

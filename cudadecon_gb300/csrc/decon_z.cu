@@ -2,6 +2,10 @@
 // inverse FFT along z.
 #include "decon_common.cuh"
 
+#ifndef CDX_Z_MINB
+#define CDX_Z_MINB 8
+#endif
+
 namespace cdx {
 
 // ---------------------------------------------------------------- z pass
@@ -17,22 +21,22 @@ static int z_cols(int nz) {
 // Last forward stage of the static z pass: multiply element e (= kz) of the
 // thread's column by the OTF, interpolated from the kz-resampled radial
 // table at the column's radius (computed once per thread), or read from the
-// precomputed 3D array.
+// precomputed 3D array.  Element e of the column's OTF is lo[e * stride].
 template <class IO>
 struct OtfColMulStore {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
   IO io;
-  const float2* lo;    // mode 0: table row ir; mode 1: the column of the 3D array
-  const float2* hi;    // mode 0: table row ir + 1
+  const float2* lo;    // mode 0: table column ir; mode 1: the column of the 3D array
   float ar;
-  int valid, full, nyp, conj;
+  int valid, full, stride, conj;
   __device__ __forceinline__ void st(int v, int e, float2 x) const {
     float2 o = make_float2(0.f, 0.f);
+    const float2* p = lo + e * stride;
     if (full) {
-      o = __ldg(lo + (long long)e * nyp);
+      o = __ldg(p);
     } else if (valid) {
-      const float2 t0 = __ldg(lo + e), t1 = __ldg(hi + e);
+      const float2 t0 = __ldg(p), t1 = __ldg(p + 1);
       o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
     }
     io.st(v, e, conj ? cmulconj(x, o) : cmul(x, o));
@@ -40,7 +44,7 @@ struct OtfColMulStore {
 };
 
 template <class Run>
-__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<8>())
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<CDX_Z_MINB>())
 k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int Wa) {
   const int W = tile_vectors<Run>(Wa);
   extern __shared__ __align__(16) float2 smem[];
@@ -69,7 +73,6 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     const int v = threadIdx.x % Run::kV;
     const int y = y0 + v;
     const float2* lo = otf.tz;
-    const float2* hi = otf.tz;
     float ar = 0.f;
     int valid = 0;
     if (otf.mode == 1) {
@@ -84,8 +87,7 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
       if (kr < (float)(otf.nr - 1)) {
         const int ir = (int)floorf(kr);
         ar = kr - (float)ir;
-        lo = otf.tz + (long long)ir * nz;
-        hi = lo + nz;
+        lo = otf.tz + ir;
         valid = 1;
       }
     }
@@ -95,7 +97,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
       Run::template run<false>(fz, W, invW, true, stw, io, io, gio);
       return;
     }
-    const OtfColMulStore<decltype(io)> ost{io, lo, hi, ar, valid, otf.mode == 1, g.nyp, conj};
+    const OtfColMulStore<decltype(io)> ost{io, lo, ar, valid, otf.mode == 1,
+                                           otf.mode == 1 ? g.nyp : otf.nr, conj};
     Run::template run<false>(fz, W, invW, true, stw, io, io, ost);
     Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
   } else {
@@ -129,8 +132,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
           if (kr < (float)(otf.nr - 1)) {
             const int ir = (int)floorf(kr);
             const float ar = kr - (float)ir;
-            const float2 t0 = __ldg(otf.tz + (long long)ir * nz + z);
-            const float2 t1 = __ldg(otf.tz + (long long)(ir + 1) * nz + z);
+            const float2 t0 = __ldg(otf.tz + (long long)z * otf.nr + ir);
+            const float2 t1 = __ldg(otf.tz + (long long)z * otf.nr + ir + 1);
             o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
           }
         }

@@ -28,7 +28,7 @@ struct OtfDev {
   int mode;           // 0: radially averaged table, 1: full 3D array in spectrum layout
   int nr;             // radial samples of the raw OTF (reference: nx_otf)
   float kxscale, kyscale;
-  const float2* tz;   // mode 0: [nr][nz] OTF resampled along kz, scaled by 1/N
+  const float2* tz;   // mode 0: [nz][nr] OTF resampled along kz, scaled by 1/N
   const float2* full; // mode 1: spectrum-layout OTF, scaled by 1/N
 };
 
