@@ -126,7 +126,7 @@ struct Session {
   DevBuf<float> pre, Xa, Xb, G, raw, rotbuf, res_stage, desk_stage, conv_tmp;
   DevBuf<float2> S;
   DevBuf<double> partials, stat_d;
-  DevBuf<unsigned> counter, stat_u;
+  DevBuf<unsigned> stat_u;
   DevBuf<float> lam;
   cudaStream_t stream = nullptr;
   long long launches = 0;
@@ -211,7 +211,6 @@ static void release_all(Session& s) {
   s.S.release();
   s.partials.release();
   s.stat_d.release();
-  s.counter.release();
   s.stat_u.release();
   s.lam.release();
   s.cc_param.release();
@@ -335,10 +334,7 @@ static int ensure_grid_buffers(Session& s, const Geom& g) {
       (rc = s.raw.ensure(n)) || (rc = s.S.ensure((size_t)g.spec_elems())))
     return rc;
   const int nblk = x_pass_blocks(g);
-  if ((rc = s.partials.ensure(2 * (size_t)nblk)) || (rc = s.counter.ensure(1)) ||
-      (rc = s.lam.ensure(2)))
-    return rc;
-  CDX_CHECK(cudaMemsetAsync(s.counter.p, 0, sizeof(unsigned), s.stream));
+  if ((rc = s.partials.ensure(2 * (size_t)nblk)) || (rc = s.lam.ensure(2))) return rc;
   CDX_CHECK(cudaMemsetAsync(s.lam.p, 0, 2 * sizeof(float), s.stream));
   return 0;
 }
@@ -348,7 +344,7 @@ static int ensure_grid_buffers(Session& s, const Geom& g) {
 // the grid of s.plan, starting from X0 in s.Xa with raw in s.raw.  Returns
 // the buffer that holds the final estimate.
 // Device buffers of one RL loop: estimates (X0 in Xa), raw, G, spectrum,
-// dot-product partials, last-block ticket and the two lambda slots.
+// dot-product partials (16 bytes per x-pass block) and the two lambda slots.
 struct LoopBufs {
   float* Xa;
   float* Xb;
@@ -356,7 +352,6 @@ struct LoopBufs {
   float* raw;
   float2* S;
   double* partials;
-  unsigned* counter;
   float* lam;
   int max_blocks;
 };
@@ -366,7 +361,6 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
   const Geom& g = p.g;
   RLWork w;
   w.partials = b.partials;
-  w.counter = b.counter;
   w.lam = b.lam;
   w.max_blocks = b.max_blocks;
   const float eps = 1.1920928955078125e-07f;  // std::numeric_limits<float>::epsilon()
@@ -407,7 +401,7 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
       return rc;
     mark();
     if (prof && g_prof.used >= 10 * 64) prof_collect();
-    *launches += 9;
+    *launches += k >= 1 ? 10 : 9;  // the update pass adds the lambda kernel
     float* t = X;
     X = Xm1;
     Xm1 = t;
@@ -417,7 +411,7 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
 }
 
 static int rl_iterations(Session& s, int nIter, float** final_x) {
-  const LoopBufs b{s.Xa.p, s.Xb.p, s.G.p, s.raw.p, s.S.p, s.partials.p, s.counter.p, s.lam.p,
+  const LoopBufs b{s.Xa.p, s.Xb.p, s.G.p, s.raw.p, s.S.p, s.partials.p, s.lam.p,
                    (int)(s.partials.n / 2)};
   return rl_loop(s.plan, b, nIter, s.stream, g_prof.on, final_x, &s.launches);
 }
@@ -702,7 +696,6 @@ struct BatchStack {
   DevBuf<float> Xa, Xb, G, raw;
   DevBuf<float2> S;
   DevBuf<double> partials;
-  DevBuf<unsigned> counter;
   DevBuf<float> lam;
   float* final_x = nullptr;
   void release() {
@@ -714,7 +707,6 @@ struct BatchStack {
     raw.release();
     S.release();
     partials.release();
-    counter.release();
     lam.release();
   }
 };
@@ -810,7 +802,7 @@ static int batch_setup_stack(BatchStack& b, const cdx_batch_stack& d, bool* chan
   if ((rc = b.raw_otf.ensure((size_t)d.otf_w * d.otf_h / 2)) || (rc = b.Xa.ensure(n)) ||
       (rc = b.Xb.ensure(n)) || (rc = b.G.ensure(n)) || (rc = b.raw.ensure(n)) ||
       (rc = b.S.ensure((size_t)g.spec_elems())) ||
-      (rc = b.partials.ensure(2 * (size_t)x_pass_blocks(g))) || (rc = b.counter.ensure(1)) ||
+      (rc = b.partials.ensure(2 * (size_t)x_pass_blocks(g))) ||
       (rc = b.lam.ensure(2)))
     return rc;
   b.os.raw_otf = b.raw_otf.p;
@@ -840,15 +832,14 @@ static int batch_capture(Batch& b, int nIters) {
     BatchStack& t = b.st[order[j]];
     cudaStream_t s = b.fan[j % K];
     const size_t n = (size_t)t.gx * t.gy * t.gz;
-    if ((e = cudaMemsetAsync(t.counter.p, 0, sizeof(unsigned), s)) != cudaSuccess ||
-        (e = cudaMemsetAsync(t.lam.p, 0, 2 * sizeof(float), s)) != cudaSuccess ||
+    if ((e = cudaMemsetAsync(t.lam.p, 0, 2 * sizeof(float), s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(t.raw.p, t.Xa.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s)) !=
             cudaSuccess) {
       set_cuda_error("batch capture", e);
       rc = e;
       break;
     }
-    const LoopBufs lb{t.Xa.p, t.Xb.p, t.G.p, t.raw.p, t.S.p, t.partials.p, t.counter.p, t.lam.p,
+    const LoopBufs lb{t.Xa.p, t.Xb.p, t.G.p, t.raw.p, t.S.p, t.partials.p, t.lam.p,
                       (int)(t.partials.n / 2)};
     rc = rl_loop(t.plan, lb, nIters, s, false, &t.final_x, &launches);
   }

@@ -1,30 +1,70 @@
 // Inverse x pass of the second convolution: C2R, estimate update and the
-// acceleration-factor dot products (last block finishes lambda).
+// acceleration-factor dot products (per-block partial sums, then a one-block
+// kernel finishes lambda).
 #include "decon_common.cuh"
 
 namespace cdx {
 
-// Block-wide sum of two doubles; result valid in thread 0.
-__device__ __forceinline__ void block_sum2(double& a, double& b, double* red) {
+// Block-wide sum of two float-float values (ah + al, bh + bl): warp shuffles,
+// then thread 0 adds the warps' sums, all with TwoSum in FP32 (GB300's FP64
+// rate is a small fraction of its FP32 rate).  Returns (sum a hi, lo, sum b
+// hi, lo), valid in thread 0.  The order of the additions is fixed, so the
+// result is the same on every run.
+__device__ __forceinline__ float4 block_sum2_ff(float ah, float al, float bh, float bl,
+                                               float4* red) {
   for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
+    const float ah2 = __shfl_down_sync(0xffffffffu, ah, o);
+    const float al2 = __shfl_down_sync(0xffffffffu, al, o);
+    const float bh2 = __shfl_down_sync(0xffffffffu, bh, o);
+    const float bl2 = __shfl_down_sync(0xffffffffu, bl, o);
+    acc_add(ah, al, ah2);
+    al = __fadd_rn(al, al2);
+    acc_add(bh, bl, bh2);
+    bl = __fadd_rn(bl, bl2);
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = (blockDim.x + 31) >> 5;
   __syncthreads();
-  if (lane == 0) {
-    red[warp] = a;
-    red[32 + warp] = b;
-  }
+  if (lane == 0) red[warp] = make_float4(ah, al, bh, bl);
   __syncthreads();
-  if (warp == 0) {
-    a = lane < nw ? red[lane] : 0.0;
-    b = lane < nw ? red[32 + lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_down_sync(0xffffffffu, a, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) {
+      const float4 r = red[w];
+      acc_add(s.x, s.y, r.x);
+      s.y = __fadd_rn(s.y, r.y);
+      acc_add(s.z, s.w, r.z);
+      s.w = __fadd_rn(s.w, r.w);
     }
+  }
+  return s;
+}
+
+// The next acceleration factor from the blocks' partial sums (one float4 per
+// update block): sums in a fixed order, then calcAccelFactor
+// (RLgpuImpl.cu:565) in double and the clamp of RL-Biggs-Andrews.cpp:298.
+// One block; launched right after the update pass, so the update blocks need
+// no fence or completion ticket.
+__global__ void __launch_bounds__(1024) k_lambda(const float4* partials, int nblk,
+                                                 float* lam_next, float eps) {
+  __shared__ float4 red[32];
+  grid_dep_wait();
+  grid_dep_launch();
+  float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    const float4 r = __ldcg(partials + i);
+    acc_add(ah, al, r.x);
+    al = __fadd_rn(al, r.y);
+    acc_add(bh, bl, r.z);
+    bl = __fadd_rn(bl, r.w);
+  }
+  const float4 s = block_sum2_ff(ah, al, bh, bl, red);
+  if (threadIdx.x == 0) {
+    const double a = (double)s.x + (double)s.y, b = (double)s.z + (double)s.w;
+    double l = a / (b + (double)eps);
+    l = (1.0 < l) ? 1.0 : l;
+    l = (l < 0.0) ? 0.0 : l;
+    *lam_next = (float)l;
   }
 }
 
@@ -79,12 +119,10 @@ struct UpdateStore {
 template <class Run>
 __global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<5>())
 k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, float* Xout,
-               float* G, int dots, double* partials, unsigned* counter, float* lam_next,
-               float eps, int Pa) {
+               float* G, int dots, float4* partials, int Pa) {
   const int P = tile_vectors<Run>(Pa);
   extern __shared__ __align__(16) float2 smem[];
-  __shared__ double red[64];
-  __shared__ bool last;
+  __shared__ float4 red[32];
   const int nx = g.nx;
   const float2* stw = Run::kGlobalTw ? fx.tw : smem;
   const auto io = Run::row_tile(smem + upd_tile_offset<Run>(nx), nx);
@@ -112,35 +150,8 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, 
   const UpdateStore us{Ys, Gs, Xout, G, dots, (long long)z * g.ny * nx, y0, g.ny, nx, acc};
   Run::template run<true>(fx, P, 1.f, false, stw, io, ld, us);
   if (!dots) return;
-  double s1 = (double)acc[0] + (double)acc[1], s2 = (double)acc[2] + (double)acc[3];
-  block_sum2(s1, s2, red);
-  const int nblk = gridDim.x * gridDim.y;
-  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-  if (threadIdx.x == 0) {
-    partials[bid] = s1;
-    partials[nblk + bid] = s2;
-    __threadfence();
-    const unsigned t = atomicAdd(counter, 1u);
-    last = (t == (unsigned)nblk - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  // Last block: reduce all partials in a fixed order (deterministic).
-  __threadfence();
-  double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
-    a += __ldcg(partials + i);
-    b += __ldcg(partials + nblk + i);
-  }
-  block_sum2(a, b, red);
-  if (threadIdx.x == 0) {
-    // calcAccelFactor (RLgpuImpl.cu:565) then the clamp of RL-Biggs-Andrews.cpp:298
-    double l = a / (b + (double)eps);
-    l = (1.0 < l) ? 1.0 : l;
-    l = (l < 0.0) ? 0.0 : l;
-    *lam_next = (float)l;
-    *counter = 0u;
-  }
+  const float4 sum = block_sum2_ff(acc[0], acc[1], acc[2], acc[3], red);
+  if (threadIdx.x == 0) partials[blockIdx.y * gridDim.x + blockIdx.x] = sum;
 }
 
 template <class Run>
@@ -155,9 +166,15 @@ static int x_update_go(const Geom& g, const FftDev& f, const float2* S, const fl
   }
   size_t smem = sizeof(float2) * ((size_t)upd_rows_offset<Run>(g.nx, P) + 2 * (size_t)P * g.nx);
   if (int rc = smem_optin(k_x_inv_update<Run>, smem)) return rc;
-  CDX_CHECK(launch_pdl(k_x_inv_update<Run>, grid, dim3(T), smem, st, g, f, S, Y, Xout, G, dots, w.partials, w.counter,
-                                             lam_next, eps, P));
+  float4* part = reinterpret_cast<float4*>(w.partials);
+  CDX_CHECK(launch_pdl(k_x_inv_update<Run>, grid, dim3(T), smem, st, g, f, S, Y, Xout, G, dots,
+                       part, P));
   CDX_LAUNCH_CHECK("k_x_inv_update");
+  if (dots) {
+    CDX_CHECK(launch_pdl(k_lambda, dim3(1), dim3(1024), 0, st, (const float4*)part, nblk, lam_next,
+                         eps));
+    CDX_LAUNCH_CHECK("k_lambda");
+  }
   return 0;
 }
 
@@ -167,7 +184,7 @@ int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const 
   if (fx.has_static) switch (g.nx) {
 #define CDX_CASE(L, PP)                                                                    \
   case L:                                                                                  \
-    return x_update_go<StaticRunner<SP##L, PP, false, true>>(g, fx.sdev, S, Y, Xout, G, dots, \
+    return x_update_go<StaticRunner<SP##L, PP, false>>(g, fx.sdev, S, Y, Xout, G, dots, \
                                                               w, lam_next, eps, PP,          \
                                                               splan_threads<SP##L, PP>(), st);
       CDX_X_PLANS(CDX_CASE)

@@ -2,10 +2,6 @@
 // inverse FFT along z.
 #include "decon_common.cuh"
 
-#ifndef CDX_Z_MINB
-#define CDX_Z_MINB 8
-#endif
-
 namespace cdx {
 
 // ---------------------------------------------------------------- z pass
@@ -44,7 +40,7 @@ struct OtfColMulStore {
 };
 
 template <class Run>
-__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<CDX_Z_MINB>())
+__global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<8>())
 k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int Wa) {
   const int W = tile_vectors<Run>(Wa);
   extern __shared__ __align__(16) float2 smem[];

@@ -55,8 +55,7 @@ bool fft_len_supported(int L);
 
 // Per-session device state for the Biggs-Andrews loop.
 struct RLWork {
-  double* partials = nullptr;   // 2 * max_blocks
-  unsigned* counter = nullptr;  // last-block ticket
+  double* partials = nullptr;   // 2 * max_blocks (16 bytes per x-pass block)
   float* lam = nullptr;         // two slots: lambda used by iteration k is lam[k & 1]
   int max_blocks = 0;
 };
@@ -82,7 +81,8 @@ int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const flo
 // Inverse x pass followed by the estimate update from the prediction Y:
 //   Xnew = max(CC*Y, 0); Gnew = Xnew - Y
 // writes Xnew into Xout (may alias Y) and Gnew into G, and when dots != 0
-// accumulates (Gnew.Gold, Gold.Gold) and stores the next lambda into lam_next.
+// accumulates (Gnew.Gold, Gold.Gold) per block, then a one-block kernel stores
+// the next lambda into lam_next.
 int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* Y,
                         float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
                         cudaStream_t st);
