@@ -93,7 +93,8 @@ struct GridPlan {
   Geom g{};
   FftLen fx, fy, fz;
   OtfDev otf{};
-  DevBuf<float2> tz, full;
+  DevBuf<float4> tz;
+  DevBuf<float2> full;
   void release() {
     fft_len_free(fx);
     fft_len_free(fy);

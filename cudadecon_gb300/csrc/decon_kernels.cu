@@ -150,20 +150,16 @@ int launch_spec_to_std(const Geom& g, const float2* S, float2* out, cudaStream_t
 
 // ---------------------------------------------------------------- OTF tables
 // Radially averaged OTF resampled along kz for every z frequency of the
-// volume: tz[z][ir] = otf[ir][iz]*(1-az) + otf[ir][iz+1 (wrapping)]*az, zero
-// where kzindex falls outside [0, nz_otf), times scale (= 1/N).  The radius
-// runs fastest, so the columns of a z tile (neighbouring ky, hence
-// neighbouring radii) gather from one or two cache lines per kz.
+// volume: t[z][ir] = otf[ir][iz]*(1-az) + otf[ir][iz+1 (wrapping)]*az, zero
+// where kzindex falls outside [0, nz_otf), times scale (= 1/N).  Stored as
+// pairs tz[z][ir] = (t[z][ir], t[z][ir+1]) so that the radial interpolation
+// of the z pass takes one 16-byte load; the radius runs fastest, so the
+// columns of a z tile (neighbouring ky, hence neighbouring radii) gather from
+// one or two cache lines per kz.
 // Follows dev_otfinterpolate's RA branch (RLgpuImpl.cu:233-273) with the kz
 // coordinate of makeOTFarray_kernel (RLgpuImpl.cu:357).
-__global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2* __restrict__ otf,
-                         float2* __restrict__ tz, float scale) {
-  const int z = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ir = blockIdx.y;
-  if (z >= nz) return;
-  const int kz = z > (nz >> 1) ? z - nz : z;
-  const float fz = (float)kz * kzscale;
-  const float kzindex = fz < 0.f ? fz + (float)nzotf : fz;
+__device__ __forceinline__ float2 otf_tz_value(int ir, int nzotf, float kzindex,
+                                               const float2* __restrict__ otf, float scale) {
   float2 v = make_float2(0.f, 0.f);
   if (kzindex < (float)nzotf && kzindex >= 0.f) {
     const int iz = (int)floorf(kzindex);
@@ -173,10 +169,24 @@ __global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2*
     const float2 b = otf[(long long)ir * nzotf + izp];
     v = make_float2(a.x * (1.f - az) + b.x * az, a.y * (1.f - az) + b.y * az);
   }
-  tz[(long long)z * nr + ir] = make_float2(v.x * scale, v.y * scale);
+  return make_float2(v.x * scale, v.y * scale);
 }
 
-int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* tz,
+__global__ void k_otf_tz(int nz, int nr, int nzotf, float kzscale, const float2* __restrict__ otf,
+                         float4* __restrict__ tz, float scale) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ir = blockIdx.y;
+  if (z >= nz) return;
+  const int kz = z > (nz >> 1) ? z - nz : z;
+  const float fz = (float)kz * kzscale;
+  const float kzindex = fz < 0.f ? fz + (float)nzotf : fz;
+  const float2 a = otf_tz_value(ir, nzotf, kzindex, otf, scale);
+  const float2 b = ir + 1 < nr ? otf_tz_value(ir + 1, nzotf, kzindex, otf, scale)
+                               : make_float2(0.f, 0.f);
+  tz[(long long)z * nr + ir] = make_float4(a.x, a.y, b.x, b.y);
+}
+
+int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float4* tz,
                   float scale, cudaStream_t st) {
   dim3 grid(ceil_div(g.nz, 128), od.nx_otf);
   k_otf_tz<<<grid, 128, 0, st>>>(g.nz, od.nx_otf, od.nz_otf, od.kzscale, raw_otf, tz, scale);

@@ -15,31 +15,34 @@ static int z_cols(int nz) {
 }
 
 // Last forward stage of the static z pass: multiply element e (= kz) of the
-// thread's column by the OTF, interpolated from the kz-resampled radial
-// table at the column's radius (computed once per thread), or read from the
-// precomputed 3D array.  Element e of the column's OTF is lo[e * stride].
-template <class IO>
+// thread's column by the OTF (conjugated when CONJ), interpolated from the
+// kz-resampled radial table at the column's radius (MODE 0: pair e of the
+// column at tz[e * nr + ir], radius computed once per thread) or read from
+// the precomputed 3D array (MODE 1: full[e * nyp]).
+template <class IO, int MODE, bool CONJ>
 struct OtfColMulStore {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
   IO io;
-  const float2* lo;    // mode 0: table column ir; mode 1: the column of the 3D array
+  const float4* lo4;  // MODE 0: table column ir
+  const float2* lo2;  // MODE 1: the column of the 3D array
   float ar;
-  int valid, full, stride, conj;
+  int valid, stride;
   __device__ __forceinline__ void st(int v, int e, float2 x) const {
     float2 o = make_float2(0.f, 0.f);
-    const float2* p = lo + e * stride;
-    if (full) {
-      o = __ldg(p);
+    if constexpr (MODE == 1) {
+      o = __ldg(lo2 + e * stride);
     } else if (valid) {
-      const float2 t0 = __ldg(p), t1 = __ldg(p + 1);
-      o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+      const float4 t = __ldg(lo4 + e * stride);
+      o = make_float2((1.f - ar) * t.x + ar * t.z, (1.f - ar) * t.y + ar * t.w);
     }
-    io.st(v, e, conj ? cmulconj(x, o) : cmul(x, o));
+    io.st(v, e, CONJ ? cmulconj(x, o) : cmul(x, o));
   }
 };
 
-template <class Run>
+// MODE and CONJ: the OTF mode and the conjugation as compile-time constants
+// (static plans), or -1 to read them from otf.mode and conj (generic engine).
+template <class Run, int MODE, int CONJ>
 __global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<8>())
 k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fwd_only, int Wa) {
   const int W = tile_vectors<Run>(Wa);
@@ -68,11 +71,12 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     // the OTF of this thread's column (the column is fixed across stages)
     const int v = threadIdx.x % Run::kV;
     const int y = y0 + v;
-    const float2* lo = otf.tz;
+    const float4* lo4 = otf.tz;
+    const float2* lo2 = otf.full;
     float ar = 0.f;
     int valid = 0;
-    if (otf.mode == 1) {
-      lo = otf.full + (long long)kx * g.plane + (y < g.ny ? y : 0);
+    if (MODE == 1) {
+      lo2 = otf.full + (long long)kx * g.plane + (y < g.ny ? y : 0);
     } else if (y < g.ny) {
       // dev_otfinterpolate RA branch (RLgpuImpl.cu:238-273): kr = sqrt(kx^2 +
       // ky^2), zero at kr >= nr-1
@@ -83,7 +87,7 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
       if (kr < (float)(otf.nr - 1)) {
         const int ir = (int)floorf(kr);
         ar = kr - (float)ir;
-        lo = otf.tz + ir;
+        lo4 = otf.tz + ir;
         valid = 1;
       }
     }
@@ -93,8 +97,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
       Run::template run<false>(fz, W, invW, true, stw, io, io, gio);
       return;
     }
-    const OtfColMulStore<decltype(io)> ost{io, lo, ar, valid, otf.mode == 1,
-                                           otf.mode == 1 ? g.nyp : otf.nr, conj};
+    const OtfColMulStore<decltype(io), MODE, CONJ == 1> ost{io, lo4, lo2, ar, valid,
+                                                            MODE == 1 ? g.nyp : otf.nr};
     Run::template run<false>(fz, W, invW, true, stw, io, io, ost);
     Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
   } else {
@@ -128,9 +132,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
           if (kr < (float)(otf.nr - 1)) {
             const int ir = (int)floorf(kr);
             const float ar = kr - (float)ir;
-            const float2 t0 = __ldg(otf.tz + (long long)z * otf.nr + ir);
-            const float2 t1 = __ldg(otf.tz + (long long)z * otf.nr + ir + 1);
-            o = make_float2((1.f - ar) * t0.x + ar * t1.x, (1.f - ar) * t0.y + ar * t1.y);
+            const float4 t = __ldg(otf.tz + (long long)z * otf.nr + ir);
+            o = make_float2((1.f - ar) * t.x + ar * t.z, (1.f - ar) * t.y + ar * t.w);
           }
         }
       }
@@ -143,7 +146,7 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
   }
 }
 
-template <class Run>
+template <class Run, int MODE, int CONJ>
 static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bool conj,
                 bool fwd_only, int W, int T, cudaStream_t st) {
   dim3 grid(ceil_div(g.ny, W), g.nxh);
@@ -151,28 +154,40 @@ static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bo
   size_t smem = Run::kStatic
                     ? sizeof(float2) * ((size_t)(g.nz + (g.nz & 1)) + (size_t)W * g.nz)
                     : fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
-  if (int rc = smem_optin(k_z_pass<Run>, smem)) return rc;
-  CDX_CHECK(launch_pdl(k_z_pass<Run>, grid, dim3(T), smem, st, g, f, S, otf, conj ? 1 : 0,
+  auto kern = k_z_pass<Run, MODE, CONJ>;
+  if (int rc = smem_optin(kern, smem)) return rc;
+  CDX_CHECK(launch_pdl(kern, grid, dim3(T), smem, st, g, f, S, otf, conj ? 1 : 0,
                        fwd_only ? 1 : 0, W));
   CDX_LAUNCH_CHECK("k_z_pass");
   return 0;
 }
 
+// Static plans: one instantiation per OTF mode and conjugation.
+template <class Run>
+static int z_go_static(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bool conj,
+                       bool fwd_only, int W, int T, cudaStream_t st) {
+  if (otf.mode == 1)
+    return conj ? z_go<Run, 1, 1>(g, f, S, otf, conj, fwd_only, W, T, st)
+                : z_go<Run, 1, 0>(g, f, S, otf, conj, fwd_only, W, T, st);
+  return conj ? z_go<Run, 0, 1>(g, f, S, otf, conj, fwd_only, W, T, st)
+              : z_go<Run, 0, 0>(g, f, S, otf, conj, fwd_only, W, T, st);
+}
+
 int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf, bool conj,
                   cudaStream_t st, bool fwd_only) {
   if (fz.has_static) switch (g.nz) {
-#define CDX_CASE(L, WW)                                                                        \
-  case L:                                                                                      \
-    return z_go<StaticRunner<SP##L, WW, true>>(g, fz.sdev, S, otf, conj, fwd_only, WW,       \
-                                               splan_threads<SP##L, WW>(), st);
+#define CDX_CASE(L, WW)                                                                    \
+  case L:                                                                                  \
+    return z_go_static<StaticRunner<SP##L, WW, true>>(g, fz.sdev, S, otf, conj, fwd_only, WW, \
+                                                       splan_threads<SP##L, WW>(), st);
       CDX_Z_PLANS(CDX_CASE)
 #undef CDX_CASE
       default:
         break;
     }
   const int W = z_cols(g.nz);
-  return z_go<GenericRunner>(g, fz.dev, S, otf, conj, fwd_only, W,
-                             threads_for((long long)W * g.nz), st);
+  return z_go<GenericRunner, -1, -1>(g, fz.dev, S, otf, conj, fwd_only, W,
+                                     threads_for((long long)W * g.nz), st);
 }
 
 }  // namespace cdx

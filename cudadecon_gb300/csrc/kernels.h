@@ -28,7 +28,8 @@ struct OtfDev {
   int mode;           // 0: radially averaged table, 1: full 3D array in spectrum layout
   int nr;             // radial samples of the raw OTF (reference: nx_otf)
   float kxscale, kyscale;
-  const float2* tz;   // mode 0: [nz][nr] OTF resampled along kz, scaled by 1/N
+  const float4* tz;   // mode 0: [nz][nr] OTF resampled along kz, scaled by 1/N, as
+                      // pairs (value at ir, value at ir + 1; 0 past the table)
   const float2* full; // mode 1: spectrum-layout OTF, scaled by 1/N
 };
 
@@ -93,7 +94,7 @@ int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* 
 int launch_spec_to_std(const Geom& g, const float2* S, float2* out, cudaStream_t st);
 
 // OTF preparation
-int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* tz,
+int launch_otf_tz(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float4* tz,
                   float scale, cudaStream_t st);
 int launch_otf_full(const Geom& g, const float2* raw_otf, const RawOtfDims& od, float2* full,
                     float scale, cudaStream_t st);
