@@ -219,12 +219,16 @@ struct RowPairLoad {
 };
 
 // First-stage loader of the forward x pass from rows prefetched into shared
-// memory (Xs, Xm1s: 2P rows of nx floats, nr of them valid).
+// memory (Xs, Xm1s: 2P rows of nx floats, nr of them valid).  With predict,
+// each element is the prediction Y = max(X + lambda (X - X_{k-1}), 0), which
+// is also stored to the block's rows Yg in global memory (the first stage
+// reads every element exactly once).
 struct RowPairSmemLoad {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
   const float* Xs;
   const float* Xm1s;
+  float* Yg;
   float lam;
   int predict, nr, nx;
   __device__ __forceinline__ float2 ld(int v, int e) const {
@@ -233,10 +237,16 @@ struct RowPairSmemLoad {
     if (ra < nr) {
       const int o = ra * nx + e;
       a = Xs[o];
-      if (predict) a = predict_y(a, Xm1s[o], lam);
+      if (predict) {
+        a = predict_y(a, Xm1s[o], lam);
+        Yg[o] = a;
+      }
       if (ra + 1 < nr) {
         b = Xs[o + nx];
-        if (predict) b = predict_y(b, Xm1s[o + nx], lam);
+        if (predict) {
+          b = predict_y(b, Xm1s[o + nx], lam);
+          Yg[o + nx] = b;
+        }
       }
     }
     return make_float2(a, b);

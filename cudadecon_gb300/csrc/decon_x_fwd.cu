@@ -34,39 +34,10 @@ k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, float* Xm1, const float*
   const float lam = predict ? __ldg(lamp) : 0.f;
   cp_async_wait_all();
   __syncthreads();
-  if (predict) {
-    // prediction of updatePrediction_kernel (RLgpuImpl.cu:658-666), kept in
-    // Xs for the transform and written over the block's rows of X_{k-1}
-    float* Yg = Xm1 + roff;
-    const int n = nr * nx;
-    if (((reinterpret_cast<unsigned long long>(Yg) | reinterpret_cast<unsigned long long>(Xm1s)) &
-         15) == 0) {
-      const int n4 = n >> 2;
-      float4* xs4 = reinterpret_cast<float4*>(Xs);
-      const float4* ms4 = reinterpret_cast<const float4*>(Xm1s);
-      float4* yg4 = reinterpret_cast<float4*>(Yg);
-      for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-        const float4 a = xs4[i], m = ms4[i];
-        const float4 y = make_float4(predict_y(a.x, m.x, lam), predict_y(a.y, m.y, lam),
-                                     predict_y(a.z, m.z, lam), predict_y(a.w, m.w, lam));
-        xs4[i] = y;
-        yg4[i] = y;
-      }
-      for (int i = 4 * n4 + threadIdx.x; i < n; i += blockDim.x) {
-        const float y = predict_y(Xs[i], Xm1s[i], lam);
-        Xs[i] = y;
-        Yg[i] = y;
-      }
-    } else {
-      for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float y = predict_y(Xs[i], Xm1s[i], lam);
-        Xs[i] = y;
-        Yg[i] = y;
-      }
-    }
-    __syncthreads();
-  }
-  const RowPairSmemLoad ld{Xs, nullptr, 0.f, 0, nr, nx};
+  // prediction of updatePrediction_kernel (RLgpuImpl.cu:658-666), applied
+  // by the first stage as it reads the rows and written over the block's
+  // rows of X_{k-1}
+  const RowPairSmemLoad ld{Xs, Xm1s, predict ? Xm1 + roff : nullptr, lam, predict, nr, nx};
   Run::template run<false>(fx, P, 1.f, false, stw, io, ld, io);
   store_half_spectra<Run::kV>(g, io, P, z, y0, S);
 }
