@@ -5,38 +5,41 @@
 
 namespace cdx {
 
-// Block-wide sum of two float-float values (ah + al, bh + bl): warp shuffles,
-// then thread 0 adds the warps' sums, all with TwoSum in FP32 (GB300's FP64
-// rate is a small fraction of its FP32 rate).  Returns (sum a hi, lo, sum b
-// hi, lo), valid in thread 0.  The order of the additions is fixed, so the
-// result is the same on every run.
+// Float-float accumulation of a second float-float value (hi, lo).
+__device__ __forceinline__ void ff_add(float4& s, float4 r) {
+  acc_add(s.x, s.y, r.x);
+  s.y = __fadd_rn(s.y, r.y);
+  acc_add(s.z, s.w, r.z);
+  s.w = __fadd_rn(s.w, r.w);
+}
+
+// Warp-wide float-float sum (tree over the lanes); result in lane 0.
+__device__ __forceinline__ float4 warp_sum2_ff(float4 s) {
+  for (int o = 16; o > 0; o >>= 1) {
+    float4 r;
+    r.x = __shfl_down_sync(0xffffffffu, s.x, o);
+    r.y = __shfl_down_sync(0xffffffffu, s.y, o);
+    r.z = __shfl_down_sync(0xffffffffu, s.z, o);
+    r.w = __shfl_down_sync(0xffffffffu, s.w, o);
+    ff_add(s, r);
+  }
+  return s;
+}
+
+// Block-wide sum of two float-float values (ah + al, bh + bl): a shuffle tree
+// in each warp, then one over the warps' sums, all with TwoSum in FP32
+// (GB300's FP64 rate is a small fraction of its FP32 rate).  Returns (sum a
+// hi, lo, sum b hi, lo), valid in thread 0.  The order of the additions is
+// fixed, so the result is the same on every run.
 __device__ __forceinline__ float4 block_sum2_ff(float ah, float al, float bh, float bl,
                                                float4* red) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const float ah2 = __shfl_down_sync(0xffffffffu, ah, o);
-    const float al2 = __shfl_down_sync(0xffffffffu, al, o);
-    const float bh2 = __shfl_down_sync(0xffffffffu, bh, o);
-    const float bl2 = __shfl_down_sync(0xffffffffu, bl, o);
-    acc_add(ah, al, ah2);
-    al = __fadd_rn(al, al2);
-    acc_add(bh, bl, bh2);
-    bl = __fadd_rn(bl, bl2);
-  }
+  float4 s = warp_sum2_ff(make_float4(ah, al, bh, bl));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = (blockDim.x + 31) >> 5;
   __syncthreads();
-  if (lane == 0) red[warp] = make_float4(ah, al, bh, bl);
+  if (lane == 0) red[warp] = s;
   __syncthreads();
-  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (threadIdx.x == 0) {
-    for (int w = 0; w < nw; ++w) {
-      const float4 r = red[w];
-      acc_add(s.x, s.y, r.x);
-      s.y = __fadd_rn(s.y, r.y);
-      acc_add(s.z, s.w, r.z);
-      s.w = __fadd_rn(s.w, r.w);
-    }
-  }
+  if (warp == 0) s = warp_sum2_ff(lane < nw ? red[lane] : make_float4(0.f, 0.f, 0.f, 0.f));
   return s;
 }
 
@@ -50,15 +53,21 @@ __global__ void __launch_bounds__(1024) k_lambda(const float4* partials, int nbl
   __shared__ float4 red[32];
   grid_dep_wait();
   grid_dep_launch();
-  float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
-    const float4 r = __ldcg(partials + i);
-    acc_add(ah, al, r.x);
-    al = __fadd_rn(al, r.y);
-    acc_add(bh, bl, r.z);
-    bl = __fadd_rn(bl, r.w);
+  // each thread sums partials t, t + T, t + 2T, ...; the loads of a batch
+  // are issued together (zeros past the end add nothing)
+  constexpr int kBatch = 8;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int i0 = threadIdx.x; i0 < nblk; i0 += kBatch * blockDim.x) {
+    float4 r[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int i = i0 + u * blockDim.x;
+      r[u] = i < nblk ? __ldcg(partials + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) ff_add(acc, r[u]);
   }
-  const float4 s = block_sum2_ff(ah, al, bh, bl, red);
+  const float4 s = block_sum2_ff(acc.x, acc.y, acc.z, acc.w, red);
   if (threadIdx.x == 0) {
     const double a = (double)s.x + (double)s.y, b = (double)s.z + (double)s.w;
     double l = a / (b + (double)eps);
