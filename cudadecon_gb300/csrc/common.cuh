@@ -41,12 +41,25 @@ __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return mak
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 // a * b
+// On the device the roundings are written out (one product rounded, the
+// other fused), so that a product computes the same value whether its
+// operands come from memory or from registers of a fused neighbouring stage.
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)),
+                     __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+#else
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+#endif
 }
 // a * conj(b)
 __host__ __device__ __forceinline__ float2 cmulconj(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+  return make_float2(__fmaf_rn(a.x, b.x, __fmul_rn(a.y, b.y)),
+                     __fmaf_rn(a.y, b.x, -__fmul_rn(a.x, b.y)));
+#else
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+#endif
 }
 __host__ __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 // multiply by -i and +i

@@ -61,6 +61,30 @@ __device__ __forceinline__ float predict_y(float x, float xm1, float lam) {
   return y > 0.f ? y : 0.f;
 }
 
+// Radial OTF interpolation (dev_otfinterpolate RA branch, RLgpuImpl.cu:238-273):
+// the column (kx, ky = y folded) lies at radius kr = |(kx kxscale, ky kyscale)|
+// of the table; zero at kr >= nr - 1.  Returns whether the column is inside,
+// with the table column ir and the fraction ar.
+__device__ __forceinline__ bool otf_radius(const OtfDev& otf, int kx, int y, int ny, int& ir,
+                                           float& ar) {
+  const int ky = y > (ny >> 1) ? y - ny : y;
+  const float fx = __fmul_rn((float)kx, otf.kxscale);
+  const float fy = __fmul_rn((float)ky, otf.kyscale);
+  const float kr = __fsqrt_rn(__fmaf_rn(fx, fx, __fmul_rn(fy, fy)));
+  if (!(kr < (float)(otf.nr - 1))) return false;
+  ir = (int)floorf(kr);
+  ar = kr - (float)ir;
+  return true;
+}
+
+// OTF value between the table pair t = (value at ir, value at ir + 1) at
+// fraction ar, with its roundings written out, so that every pass computes
+// the same value.
+__device__ __forceinline__ float2 otf_lerp(float4 t, float ar) {
+  const float a0 = __fsub_rn(1.f, ar);
+  return make_float2(__fmaf_rn(ar, t.z, __fmul_rn(a0, t.x)), __fmaf_rn(ar, t.w, __fmul_rn(a0, t.y)));
+}
+
 // Split the FFT Z of packed rows (a + i b) into the half spectra of a and b.
 __device__ __forceinline__ float4 split_pair(float2 zk, float2 zm) {
   // A = (Z[k] + conj(Z[n-k]))/2, B = (Z[k] - conj(Z[n-k]))/(2i)

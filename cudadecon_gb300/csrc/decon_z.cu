@@ -33,8 +33,7 @@ struct OtfColMulStore {
     if constexpr (MODE == 1) {
       o = __ldg(lo2 + e * stride);
     } else if (valid) {
-      const float4 t = __ldg(lo4 + e * stride);
-      o = make_float2((1.f - ar) * t.x + ar * t.z, (1.f - ar) * t.y + ar * t.w);
+      o = otf_lerp(__ldg(lo4 + e * stride), ar);
     }
     io.st(v, e, CONJ ? cmulconj(x, o) : cmul(x, o));
   }
@@ -78,15 +77,8 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     if (MODE == 1) {
       lo2 = otf.full + (long long)kx * g.plane + (y < g.ny ? y : 0);
     } else if (y < g.ny) {
-      // dev_otfinterpolate RA branch (RLgpuImpl.cu:238-273): kr = sqrt(kx^2 +
-      // ky^2), zero at kr >= nr-1
-      const int ky = y > (g.ny >> 1) ? y - g.ny : y;
-      const float fx = (float)kx * otf.kxscale;
-      const float fy = (float)ky * otf.kyscale;
-      const float kr = sqrtf(fx * fx + fy * fy);
-      if (kr < (float)(otf.nr - 1)) {
-        const int ir = (int)floorf(kr);
-        ar = kr - (float)ir;
+      int ir = 0;
+      if (otf_radius(otf, kx, y, g.ny, ir, ar)) {
         lo4 = otf.tz + ir;
         valid = 1;
       }
@@ -125,16 +117,10 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
         if (otf.mode == 1) {
           o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
         } else {
-          const int ky = y > (g.ny >> 1) ? y - g.ny : y;
-          const float fx = (float)kx * otf.kxscale;
-          const float fy = (float)ky * otf.kyscale;
-          const float kr = sqrtf(fx * fx + fy * fy);
-          if (kr < (float)(otf.nr - 1)) {
-            const int ir = (int)floorf(kr);
-            const float ar = kr - (float)ir;
-            const float4 t = __ldg(otf.tz + (long long)z * otf.nr + ir);
-            o = make_float2((1.f - ar) * t.x + ar * t.z, (1.f - ar) * t.y + ar * t.w);
-          }
+          int ir = 0;
+          float ar = 0.f;
+          if (otf_radius(otf, kx, y, g.ny, ir, ar))
+            o = otf_lerp(__ldg(otf.tz + (long long)z * otf.nr + ir), ar);
         }
       }
       otf_tile[idx] = o;
