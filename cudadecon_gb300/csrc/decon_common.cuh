@@ -211,37 +211,6 @@ __device__ __forceinline__ void prefetch_packed_spectra(const Geom& g, const flo
 }
 
 // ---------------------------------------------------------------- stage I/O
-// Outputs per load batch of the fused epilogues (bounds their registers).
-constexpr int kStoreBatch = 4;
-
-// First-stage loader of the forward x pass: row pair v of the tile (rows
-// y0+2v and y0+2v+1 of slice z) packed as a + i b, with the prediction
-// Y = max(X + lambda (X - X_{k-1}), 0) applied on the fly when predict != 0.
-struct RowPairLoad {
-  static constexpr bool kSmem = false;
-  static constexpr bool kGroup = false;
-  const float* X;
-  const float* Xm1;
-  float lam;
-  int predict;
-  long long zoff;
-  int y0, ny, nx;
-  __device__ __forceinline__ float2 ld(int v, int e) const {
-    const int ya = y0 + 2 * v;
-    float a = 0.f, b = 0.f;
-    if (ya < ny) {
-      const long long o = zoff + (long long)ya * nx + e;
-      a = __ldg(X + o);
-      if (predict) a = predict_y(a, __ldg(Xm1 + o), lam);
-      if (ya + 1 < ny) {
-        b = __ldg(X + o + nx);
-        if (predict) b = predict_y(b, __ldg(Xm1 + o + nx), lam);
-      }
-    }
-    return make_float2(a, b);
-  }
-};
-
 // First-stage loader of the forward x pass from rows prefetched into shared
 // memory (Xs, Xm1s: 2P rows of nx floats, nr of them valid).  With predict,
 // each element is the prediction Y = max(X + lambda (X - X_{k-1}), 0), which
