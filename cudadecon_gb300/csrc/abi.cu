@@ -125,6 +125,11 @@ struct Session {
   GridPlan plan;
   DevBuf<unsigned short> u16in;
   DevBuf<float> pre, Xa, Xb, G, raw, rotbuf, res_stage, desk_stage, conv_tmp;
+  // Y tiling (cdx_RL_tiled): the whole raw stack, one tile, the stitched
+  // output and its blend weights
+  DevBuf<unsigned short> tile_raw, tile_in;
+  DevBuf<float> tile_out;
+  DevBuf<unsigned char> tile_weight;
   DevBuf<float2> S;
   DevBuf<double> partials, stat_d;
   DevBuf<unsigned> stat_u;
@@ -209,6 +214,10 @@ static void release_all(Session& s) {
   s.res_stage.release();
   s.desk_stage.release();
   s.conv_tmp.release();
+  s.tile_raw.release();
+  s.tile_in.release();
+  s.tile_out.release();
+  s.tile_weight.release();
   s.S.release();
   s.partials.release();
   s.stat_d.release();
@@ -1112,6 +1121,10 @@ void RL_cleanup(void) {
   s.desk_stage.release();
   s.res_stage.release();
   s.conv_tmp.release();
+  s.tile_raw.release();
+  s.tile_in.release();
+  s.tile_out.release();
+  s.tile_weight.release();
 }
 
 void cuda_reset(void) {
@@ -1461,9 +1474,10 @@ int cdx_RL_tiled(const unsigned short* raw, int nx, int ny, int nz, float* resul
   if (ensure_stream(s)) return 0;
   cudaStream_t st = s.stream;
   const size_t tvox = (size_t)nx * tile_size * nz;
-  DevBuf<unsigned short> d_raw, d_tile;
-  DevBuf<float> stitch;
-  DevBuf<unsigned char> weight;
+  DevBuf<unsigned short>& d_raw = s.tile_raw;
+  DevBuf<unsigned short>& d_tile = s.tile_in;
+  DevBuf<float>& stitch = s.tile_out;
+  DevBuf<unsigned char>& weight = s.tile_weight;
   int onx = 0, ony_total = 0, onz = 0;
   // the raw stack goes to the device once; each tile's rows are gathered there
   int ok = d_raw.ensure((size_t)nx * ny * nz) == 0 && d_tile.ensure(tvox) == 0 &&
@@ -1509,10 +1523,6 @@ int cdx_RL_tiled(const unsigned short* raw, int nx, int ny, int nz, float* resul
          cudaStreamSynchronize(st) == cudaSuccess;
   else
     cudaStreamSynchronize(st);
-  d_raw.release();
-  d_tile.release();
-  stitch.release();
-  weight.release();
   return ok;
 }
 

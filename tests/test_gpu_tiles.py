@@ -59,3 +59,18 @@ def test_mip_matches_max(cdx, torch_cuda, axis):
     dim = {0: 2, 1: 1, 2: 0}[axis]
     want = torch.clamp_min(v.max(dim=dim).values, -1e10)
     assert torch.equal(got, want)
+
+
+def test_tiled_repeat_calls_reuse_buffers(cdx, torch_cuda, tmp_path):
+    """The tiling buffers stay in the session between calls: a second call
+    (and one on a different stack) must not see the first call's stitch
+    weights or output."""
+    a = synth.bead_stack((12, 90, 40), n_beads=20, seed=51)
+    b = synth.bead_stack((12, 90, 40), n_beads=25, seed=52)
+    _init(cdx, tmp_path, (12, 40, 40))
+    ra1 = cdx.rl_tiled(a, tile=40, tile_overlap=12, blend=True, n_iters=3)
+    rb = cdx.rl_tiled(b, tile=40, tile_overlap=12, blend=True, n_iters=3)
+    ra2 = cdx.rl_tiled(a, tile=40, tile_overlap=12, blend=True, n_iters=3)
+    cdx.rl_cleanup()
+    assert np.array_equal(ra1, ra2)
+    assert not np.array_equal(ra1, rb)
