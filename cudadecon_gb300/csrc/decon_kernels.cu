@@ -101,17 +101,26 @@ int fft_len_init(FftLen& f, int L) {
   if (f.has_static) {
     if (int rc = build_fft_dev(L, rad, f.sdev, &f.d_tws)) return rc;
   }
+  int pairs = 0;
+  f.has_xr = xr_radices(L, rad, pairs);
+  if (f.has_xr) {
+    if (int rc = build_fft_dev(L, rad, f.xrdev, &f.d_twxr)) return rc;
+  }
   return 0;
 }
 
 void fft_len_free(FftLen& f) {
   if (f.d_tw) cudaFree(f.d_tw);
   if (f.d_tws) cudaFree(f.d_tws);
+  if (f.d_twxr) cudaFree(f.d_twxr);
   f.d_tw = nullptr;
   f.d_tws = nullptr;
+  f.d_twxr = nullptr;
   f.dev.tw = nullptr;
   f.sdev.tw = nullptr;
+  f.xrdev.tw = nullptr;
   f.has_static = false;
+  f.has_xr = false;
 }
 
 // Row pairs per block of the x passes: the registered tile of a compile-time
@@ -128,7 +137,15 @@ static int x_tile_pairs(int nx) {
   }
 }
 
-int x_pass_blocks(const Geom& g) { return ceil_div(g.ny, 2 * x_tile_pairs(g.nx)) * g.nz; }
+// Blocks of the x pass with the most (the smallest tile): the dot-product
+// partials are sized by it.
+int x_pass_blocks(const Geom& g) {
+  int p = x_tile_pairs(g.nx);
+  std::vector<int> rad;
+  int pxr = 0;
+  if (xr_radices(g.nx, rad, pxr) && pxr < p) p = pxr;
+  return ceil_div(g.ny, 2 * p) * g.nz;
+}
 
 __global__ void k_spec_to_std(Geom g, const float2* __restrict__ S, float2* __restrict__ out) {
   const long long n = (long long)g.nz * g.ny * g.nxh;

@@ -49,6 +49,16 @@ static int x_ratio_go(const Geom& g, const FftDev& f, float2* S, const float* ra
 
 int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const float* raw,
                            float eps, cudaStream_t st) {
+  if (fx.has_xr) switch (g.nx) {
+#define CDX_XR_CASE(L, PP, ...)                                                            \
+  case L:                                                                                  \
+    return x_ratio_go<StaticRunner<SPR##L, PP, false>>(g, fx.xrdev, S, raw, eps, PP,       \
+                                                       splan_threads<SPR##L, PP>(), st);
+      CDX_XR_PLANS(CDX_XR_CASE)
+#undef CDX_XR_CASE
+      default:
+        break;
+    }
   if (fx.has_static) switch (g.nx) {
 #define CDX_CASE(L, PP) \
   case L:               \

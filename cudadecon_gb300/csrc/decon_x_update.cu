@@ -190,6 +190,17 @@ static int x_update_go(const Geom& g, const FftDev& f, const float2* S, const fl
 int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* Y,
                         float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
                         cudaStream_t st) {
+  if (fx.has_xr) switch (g.nx) {
+#define CDX_XR_CASE(L, PP, ...)                                                                 \
+  case L:                                                                                       \
+    return x_update_go<StaticRunner<SPR##L, PP, false>>(g, fx.xrdev, S, Y, Xout, G, dots, w,    \
+                                                        lam_next, eps, PP,                      \
+                                                        splan_threads<SPR##L, PP>(), st);
+      CDX_XR_PLANS(CDX_XR_CASE)
+#undef CDX_XR_CASE
+      default:
+        break;
+    }
   if (fx.has_static) switch (g.nx) {
 #define CDX_CASE(L, PP)                                                                    \
   case L:                                                                                  \

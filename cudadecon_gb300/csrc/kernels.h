@@ -49,6 +49,10 @@ struct FftLen {
   bool has_static = false;
   FftDev sdev;
   float2* d_tws = nullptr;
+  // the x ratio / x update plan where it differs from the registered one
+  bool has_xr = false;
+  FftDev xrdev;
+  float2* d_twxr = nullptr;
 };
 int fft_len_init(FftLen& f, int L);
 void fft_len_free(FftLen& f);

@@ -23,6 +23,13 @@
   F(1024, 32, 32)         \
   F(1620, 15, 12, 9)
 
+// Plans for the x ratio and x update passes where they differ from the
+// length's registered plan: F(L, P, radices...).  1024 = 32*32 gives a row
+// pair 32 threads of 32 values, and those two passes, which stage several
+// row arrays per tile, then fit few warps per SM; 8*16*8 with two pairs per
+// block holds 16 values per thread in a 256-thread block.
+#define CDX_XR_PLANS(F) F(1024, 2, 8, 16, 8)
+
 #define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 2) F(1024, 4) F(1620, 2)
 #define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 2)
 #define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
@@ -33,11 +40,19 @@ namespace cdx {
 CDX_SPLAN_LIST(CDX_DEF_SPLAN)
 #undef CDX_DEF_SPLAN
 
+#define CDX_DEF_XRPLAN(L, P, ...) using SPR##L = SPlan<L, __VA_ARGS__>;
+CDX_XR_PLANS(CDX_DEF_XRPLAN)
+#undef CDX_DEF_XRPLAN
+
 #define CDX_FIT_ROWS(L, V) \
   static_assert(splan_rows_fit<SP##L, V>(), "row tile too small for the static plan of length " #L);
 CDX_X_PLANS(CDX_FIT_ROWS)
 CDX_Y_PLANS(CDX_FIT_ROWS)
 #undef CDX_FIT_ROWS
+#define CDX_FIT_XR(L, P, ...) \
+  static_assert(splan_rows_fit<SPR##L, P>(), "row tile too small for the x ratio plan of " #L);
+CDX_XR_PLANS(CDX_FIT_XR)
+#undef CDX_FIT_XR
 
 // Radices of the registered plan for length L (false when L is not registered).
 inline bool static_radices(int L, std::vector<int>& rad) {
@@ -48,6 +63,22 @@ inline bool static_radices(int L, std::vector<int>& rad) {
     return true;
     CDX_SPLAN_LIST(CDX_RAD_CASE)
 #undef CDX_RAD_CASE
+    default:
+      return false;
+  }
+}
+
+// Radices and row pairs of the x ratio / x update plan for length L (false
+// when those passes use the length's registered plan).
+inline bool xr_radices(int L, std::vector<int>& rad, int& pairs) {
+  switch (L) {
+#define CDX_XR_CASE(LL, PP, ...) \
+  case LL:                       \
+    rad = {__VA_ARGS__};         \
+    pairs = PP;                  \
+    return true;
+    CDX_XR_PLANS(CDX_XR_CASE)
+#undef CDX_XR_CASE
     default:
       return false;
   }

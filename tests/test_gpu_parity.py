@@ -123,6 +123,23 @@ def test_rl_interface_matches_oracle(cdx, oracle, torch_cuda, tmp_path, case):
     cdx.rl_cleanup()
 
 
+@pytest.mark.parametrize("nx", [128, 256, 512, 756, 1024, 1620])
+def test_rl_registered_x_lengths_match_oracle(cdx, oracle, torch_cuda, tmp_path, nx):
+    """Every compile-time x plan through the whole loop (prediction, ratio,
+    update and dot products); 1024 runs its ratio and update passes on their
+    own 8*16*8 plan."""
+    shape = (12, 24, nx)
+    raw = synth.bead_stack(shape, n_beads=30, psf_sigma_xy=1.2, psf_sigma_z=1.5, seed=nx)
+    tab = synth.gaussian_otf_table(nx // 2 + 1, 12, 1.2, 2.0)
+    _init(cdx, tmp_path, shape, tab)
+    assert cdx.decon_grid() == shape
+    out = cdx.rl_decon(raw, background=100.0, n_iters=6)
+    st = _oracle_state(oracle, shape, tab)
+    ref, _ = oracle.rl_interface(st, raw, background=100.0, nIters=6)
+    cdx.rl_cleanup()
+    assert rel_l2(out, ref) < RL_TOL
+
+
 def test_rl_bleach_rescale_state(cdx, oracle, torch_cuda, tmp_path):
     shape = (16, 40, 48)
     tab = synth.gaussian_otf_table(25, 16, 1.2, 2.0)
