@@ -31,7 +31,7 @@
 #define CDX_XR_PLANS(F) F(1024, 2, 8, 16, 8)
 
 #define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 2) F(1024, 4) F(1620, 2)
-#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 2)
+#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 4)
 #define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
 
 namespace cdx {
