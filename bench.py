@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import datetime
 import json
 import math
 import os
@@ -77,9 +78,12 @@ def make_inputs(tmpdir):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """nvidia-smi clock/throttle sampling of the timed region.  Sampling starts
+    before the warm-up (nvidia-smi takes a while to produce its first row) at
+    50 ms; the samples time-stamped inside the timed region are kept, or, when
+    the region is shorter than the interval, the ones nearest to it."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -93,12 +97,14 @@ class ClockSampler:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
-    def stop(self):
+    def stop(self, t0=None, t1=None):
+        """Summary of the samples time-stamped within [t0, t1] (wall-clock
+        seconds), else of the two nearest to that window."""
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -109,6 +115,20 @@ class ClockSampler:
         self.f.flush()
         rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
         os.unlink(self.f.name)
+        if t0 is not None and t1 is not None and rows:
+            def stamp(r):
+                try:
+                    return datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except (ValueError, IndexError):
+                    return None
+            timed = [(stamp(r), r) for r in rows]
+            timed = [(t, r) for t, r in timed if t is not None]
+            inside = [r for t, r in timed if t0 <= t <= t1]
+            if inside:
+                rows = inside
+            elif timed:
+                mid = 0.5 * (t0 + t1)
+                rows = [r for _, r in sorted(timed, key=lambda tr: abs(tr[0] - mid))[:2]]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
@@ -329,6 +349,8 @@ def run_gb300(args):
             raise RuntimeError(L.cdx_last_error().decode())
 
     torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
@@ -336,11 +358,10 @@ def run_gb300(args):
     launches_per_step = int(L.cdx_last_launch_count())
     grid_vox = gz * gy * gx
     # ---- timed region (device-resident inputs)
-    clk = ClockSampler(local)
-    clk.start()
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
+    t_wall0 = time.time()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -349,8 +370,9 @@ def run_gb300(args):
     e1.record(stream)
     e1.synchronize()
     torch.cuda.synchronize()
+    t_wall1 = time.time()
     dev_ms = e0.elapsed_time(e1)
-    clocks = clk.stop()
+    clocks = clk.stop(t_wall0, t_wall1)
     dev_ms = max_over_ranks(dev_ms, pg, dev)
     ms_per_step = dev_ms / args.steps
     vox_iters = grid_vox * n_iters
