@@ -40,7 +40,7 @@ def test_find_optimal_dimension_known_values(oracle):
         assert all(oracle.not_good_dimension(k) for k in range(m + 1, n + 1))
 
 
-def test_stage_scan_geometry_matches_survey_numbers(oracle):
+def test_stage_scan_geometry_known_answers(oracle):
     # 101x256x512 raw at 31.5 deg, dz 0.3, dxy 0.104 -> decon 100x256x756, rotated 150x256x723
     tab = synth.gaussian_otf_table(129, 64, 1.3, 3.0)
     st = _state(oracle, (101, 256, 512), tab, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.2,
