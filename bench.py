@@ -250,7 +250,7 @@ BATCH = {"stacks": 64, "iterations": 10, "seed": 1003, "z": (32, 160), "y": (128
 
 
 def run_batch(cdx, dev, reps=3):
-    """Config 4: uneven stacks with their own OTFs through cdx_RL_batch_device
+    """64 uneven stacks with their own OTFs through cdx_RL_batch_device
     (one CUDA graph per call), and the same stacks through per-stack calls
     (RL_interface_init + cdx_RL_device each) for comparison.  Stacks are a
     Poisson background plus sparse point beads, generated on the GPU (seeded);

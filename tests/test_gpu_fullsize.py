@@ -1,6 +1,6 @@
 """Full-size checks where the oracle would take too long: size-independent
-properties of the RL pipeline at config 5's grid (256x1024x1024 u16 raw,
-deskewed to 256x1024x1620).
+properties of the RL pipeline on the large time-lapse stack's grid
+(256x1024x1024 u16 raw, deskewed to 256x1024x1620).
 
 With a unit OTF the blur is the identity, so the RL ratio is raw / X and a
 run started from the conditioned stack stays there: the result must equal the
@@ -15,7 +15,7 @@ from cudadecon_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def test_unit_otf_is_a_fixed_point_at_config5_size(cdx, oracle, torch_cuda, tmp_path):
+def test_unit_otf_is_a_fixed_point_at_256x1024x1620(cdx, oracle, torch_cuda, tmp_path):
     torch = torch_cuda
     shape = (256, 1024, 1024)
     nz, ny, nx = shape

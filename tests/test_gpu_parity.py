@@ -70,8 +70,8 @@ def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
 
 @pytest.mark.parametrize("shape", [(16, 32, 30), (20, 24, 45), (64, 256, 256), (100, 256, 756),
                                    (128, 128, 128), (32, 512, 1024),
-                                   (16, 40, 1620),     # registered x length of config 5
-                                   (128, 512, 1024)])  # the last is config 3's full grid
+                                   (16, 40, 1620),     # registered x length (deskewed 1024)
+                                   (128, 512, 1024)])  # the 128x512x1024 precision-study grid
 @pytest.mark.parametrize("conj", [0, 1])
 def test_conv3d_matches_oracle(cdx, oracle, torch_cuda, tmp_path, shape, conj):
     torch = torch_cuda

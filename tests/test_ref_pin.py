@@ -114,21 +114,21 @@ def _rl_case(cdx, ref, oracle, tmp_path, raw, tab, n_iters, init_kw, background=
 
 
 def test_rl_plain_64x256x256_vs_reference(cdx, ref, oracle, tmp_path):
-    # BASELINE config 1 shape: 10 iterations, background 100, no deskew
+    # the 64x256x256 bead stack: 10 iterations, background 100, no deskew
     raw = synth.bead_stack((64, 256, 256), n_beads=200, seed=1001)
     tab = synth.gaussian_otf_table(129, 64, 1.5, 4.0)
     mine, theirs, fp64, lam = _rl_case(cdx, ref, oracle, tmp_path, raw, tab, 10,
                                        dict(dr=0.1, dz=0.2, dr_psf=0.1, dz_psf=0.2))
     e_ref = rel_l2(mine, theirs)
     e64, e64_ref = rel_l2(mine, fp64), rel_l2(theirs, fp64)
-    print(f"\nC1 64x256x256 10 it: rel L2 vs reference {e_ref:.2e}; vs FP64: ours {e64:.2e}, "
+    print(f"\nbeads 64x256x256 10 it: rel L2 vs reference {e_ref:.2e}; vs FP64: ours {e64:.2e}, "
           f"reference {e64_ref:.2e}; lambdas {np.round(lam, 4).tolist()}")
     assert e_ref < 1e-5
     assert e64 < 1e-4
 
 
 def test_rl_stage_scan_deskewed_vs_reference(cdx, ref, oracle, tmp_path):
-    # BASELINE config 2: deskew 31.5 deg to 100x256x756, 15 iterations
+    # the stage-scan stack: deskew 31.5 deg to 100x256x756, 15 iterations
     raw = synth.bead_stack((101, 256, 512), n_beads=300, psf_sigma_xy=1.3, psf_sigma_z=3.0,
                            n_filaments=12, seed=1002)
     tab = synth.gaussian_otf_table(129, 64, 1.3, 3.0)
@@ -137,7 +137,7 @@ def test_rl_stage_scan_deskewed_vs_reference(cdx, ref, oracle, tmp_path):
                                             deskew_angle=31.5))
     e_ref = rel_l2(mine, theirs)
     e64, e64_ref = rel_l2(mine, fp64), rel_l2(theirs, fp64)
-    print(f"\nC2 100x256x756 15 it: rel L2 vs reference {e_ref:.2e}; vs FP64: ours {e64:.2e}, "
+    print(f"\nstage-scan 100x256x756 15 it: rel L2 vs reference {e_ref:.2e}; vs FP64: ours {e64:.2e}, "
           f"reference {e64_ref:.2e}; lambdas {np.round(lam, 4).tolist()}")
     assert e_ref < 1e-5
     assert e64 < 1e-4
