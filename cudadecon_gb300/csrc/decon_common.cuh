@@ -215,7 +215,9 @@ __device__ __forceinline__ void prefetch_packed_spectra(const Geom& g, const flo
 // memory (Xs, Xm1s: 2P rows of nx floats, nr of them valid).  With predict,
 // each element is the prediction Y = max(X + lambda (X - X_{k-1}), 0), which
 // is also stored to the block's rows Yg in global memory (the first stage
-// reads every element exactly once).
+// reads every element exactly once).  Y is read again only by the update
+// pass at the end of the iteration, so it is stored evict-first (__stcs),
+// leaving the L2 to the spectrum the y pass reads next.
 struct RowPairSmemLoad {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
@@ -232,13 +234,13 @@ struct RowPairSmemLoad {
       a = Xs[o];
       if (predict) {
         a = predict_y(a, Xm1s[o], lam);
-        Yg[o] = a;
+        __stcs(Yg + o, a);
       }
       if (ra + 1 < nr) {
         b = Xs[o + nx];
         if (predict) {
           b = predict_y(b, Xm1s[o + nx], lam);
-          Yg[o + nx] = b;
+          __stcs(Yg + o + nx, b);
         }
       }
     }

@@ -115,8 +115,9 @@ struct UpdateStore {
       acc_add(acc[2], acc[3], __fmul_rn(go, go));
     }
     const long long o = zoff + (long long)(y0 + rloc) * nx + e;
-    Xout[o] = xn;
-    G[o] = gn;
+    // read again only in the next iteration's x passes: evict-first
+    __stcs(Xout + o, xn);
+    __stcs(G + o, gn);
   }
   __device__ __forceinline__ void st(int v, int e, float2 c) const {
     const int ya = y0 + 2 * v;
