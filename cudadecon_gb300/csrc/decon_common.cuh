@@ -163,9 +163,35 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// L2 policy that marks lines evict-first.  The x passes copy the real arrays
+// they read once per iteration (X, X_{k-1}, the raw stack, Y, G_{k-1}) with
+// it, so those lines leave the L2 before the spectrum the kernel writes,
+// which the next y pass reads.
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void cp_async16_ef(void* dst, const void* src, unsigned long long pol) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src),
+               "l"(pol)
+               : "memory");
+}
+
 // Copy count floats from src (global) to dst (shared); 16-byte copies when
-// both addresses allow them, 4-byte copies otherwise.
-__device__ __forceinline__ void prefetch_floats(float* dst, const float* src, int count) {
+// both addresses allow them, 4-byte copies otherwise.  With ef, the 16-byte
+// copies leave their lines evict-first in L2.
+__device__ __forceinline__ void prefetch_floats(float* dst, const float* src, int count,
+                                                bool ef = false) {
+  if (ef && ((reinterpret_cast<unsigned long long>(src) | reinterpret_cast<unsigned long long>(dst)) &
+             15) == 0) {
+    const unsigned long long pol = l2_evict_first_policy();
+    const int n4 = count >> 2;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) cp_async16_ef(dst + 4 * i, src + 4 * i, pol);
+    for (int i = 4 * n4 + threadIdx.x; i < count; i += blockDim.x) cp_async4(dst + i, src + i);
+    return;
+  }
   if (((reinterpret_cast<unsigned long long>(src) | reinterpret_cast<unsigned long long>(dst)) &
        15) == 0) {
     const int n4 = count >> 2;

@@ -28,8 +28,8 @@ k_x_fwd(Geom g, FftDev fx, const float* __restrict__ X, float* Xm1, const float*
   load_twiddles(fx, stw);
   grid_dep_wait();
   grid_dep_launch();
-  prefetch_floats(Xs, X + roff, nr * nx);
-  if (predict) prefetch_floats(Xm1s, Xm1 + roff, nr * nx);
+  prefetch_floats(Xs, X + roff, nr * nx, true);
+  if (predict) prefetch_floats(Xm1s, Xm1 + roff, nr * nx, true);
   cp_async_commit();
   const float lam = predict ? __ldg(lamp) : 0.f;
   cp_async_wait_all();

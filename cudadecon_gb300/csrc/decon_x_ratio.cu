@@ -25,7 +25,7 @@ k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __rest
   grid_dep_wait();
   grid_dep_launch();
   prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
-  prefetch_floats(raws, raw + ((long long)z * g.ny + y0) * nx, nr * nx);
+  prefetch_floats(raws, raw + ((long long)z * g.ny + y0) * nx, nr * nx, true);
   cp_async_commit();
   cp_async_wait_all();
   __syncthreads();

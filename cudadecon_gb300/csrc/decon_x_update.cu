@@ -150,8 +150,8 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, 
   grid_dep_wait();
   grid_dep_launch();
   prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
-  prefetch_floats(Ys, Y + roff, nr * nx);
-  if (dots) prefetch_floats(Gs, G + roff, nr * nx);
+  prefetch_floats(Ys, Y + roff, nr * nx, true);
+  if (dots) prefetch_floats(Gs, G + roff, nr * nx, true);
   cp_async_commit();
   cp_async_wait_all();
   __syncthreads();
