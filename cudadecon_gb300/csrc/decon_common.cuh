@@ -224,15 +224,21 @@ __host__ __device__ __forceinline__ int x_rows_offset(int nx, int P) {
 // the P pairs of one kx (a contiguous run of 16P bytes in S).
 template <int PC>
 __device__ __forceinline__ void prefetch_packed_spectra(const Geom& g, const float2* S, float4* stg,
-                                                        int P, int z, int y0) {
+                                                        int P, int z, int y0, bool ef = false) {
   const int nxh = g.nxh;
   const int n = nxh * P;
   const float invP = 1.f / (float)P;
   const long long zo = (long long)z * g.nyp + y0;
+  const unsigned long long pol = ef ? l2_evict_first_policy() : 0ull;
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     int p, k;
     divmod_small<PC>(idx, P, invP, k, p);
-    if (y0 + 2 * p < g.ny) cp_async16(stg + p * nxh + k, S + (long long)k * g.plane + zo + 2 * p);
+    if (y0 + 2 * p < g.ny) {
+      if (ef)
+        cp_async16_ef(stg + p * nxh + k, S + (long long)k * g.plane + zo + 2 * p, pol);
+      else
+        cp_async16(stg + p * nxh + k, S + (long long)k * g.plane + zo + 2 * p);
+    }
   }
 }
 

@@ -115,8 +115,9 @@ struct UpdateStore {
       acc_add(acc[2], acc[3], __fmul_rn(go, go));
     }
     const long long o = zoff + (long long)(y0 + rloc) * nx + e;
-    // read again only in the next iteration's x passes: evict-first
-    __stcs(Xout + o, xn);
+    // X is read next by the x forward pass (kept in L2); G only by the next
+    // iteration's update pass (evict-first)
+    Xout[o] = xn;
     __stcs(G + o, gn);
   }
   __device__ __forceinline__ void st(int v, int e, float2 c) const {
@@ -149,7 +150,8 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, 
   if (!Run::kGlobalTw) load_twiddles(fx, smem);
   grid_dep_wait();
   grid_dep_launch();
-  prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0);
+  // the last read of this iteration's spectrum: evict-first
+  prefetch_packed_spectra<Run::kV>(g, S, stg, P, z, y0, true);
   prefetch_floats(Ys, Y + roff, nr * nx, true);
   if (dots) prefetch_floats(Gs, G + roff, nr * nx, true);
   cp_async_commit();
