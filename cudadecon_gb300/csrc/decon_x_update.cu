@@ -91,7 +91,8 @@ __host__ __device__ __forceinline__ int upd_rows_offset(int nx, int P) {
 // Last inverse stage: estimate update (currEstimate_kernel +
 // currPrevDiff_kernel, RLgpuImpl.cu:462-470, 501-508) from the prediction Y,
 // with the Biggs-Andrews dot products of innerProduct_kernel
-// (RLgpuImpl.cu:571-633: float products, double sums).
+// (RLgpuImpl.cu:571-633: float products summed in double there; here in
+// float-float, about 48 significant bits).
 struct UpdateStore {
   static constexpr bool kSmem = false;
   static constexpr bool kGroup = false;
