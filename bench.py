@@ -10,16 +10,19 @@ subtraction, deskew, 15 RL iterations, rotation.
   value : inputs already resident in HBM, cdx_RL_device on a stream, timed
           with CUDA events (device time), voxel-iterations/s of the decon grid
   e2e   : RL_interface (the reference's C entry point) with pinned host
-          buffers, host<->device copies inside the timed region
+          buffers, host<->device copies inside the timed region; also with
+          pageable numpy buffers (e2e.pageable)
   roofline : one RL iteration against the measured HBM copy bandwidth, with
           56 B of algorithmic traffic per voxel-iteration, timed per pass with
           CUDA events recorded by the library on its launch stream
   cpu_baseline : the CPU restatement (scipy.fft float32, all host cores) on
-          a bounded sample (2 of the 15 iterations) of the same volume
+          a bounded sample (at least 10 s of iterations) of the same volume
 
---impl reference times the reference path on the host CPU.  The reference
-has no CPU implementation of this loop (its RL runs only through cuFFT on a
-GPU), so the timed CPU arm is the restatement of that loop in oracle/.
+--impl reference times the reference's own implementation of the path: its
+CUDA kernels (compiled to PTX from its sources) with cuFFT, launched in the
+order of RichardsonLucy_GPU's host code on the same workload (the reference
+has no CPU implementation of this loop).  cpu_baseline, in both arms, is the
+CPU restatement in oracle/ (scipy.fft float32, all host cores).
 
 Multi-GPU: independent stacks do not exchange data, so N ranks run N
 replicas (weak scaling); value is the work of all ranks over the slowest
@@ -206,7 +209,40 @@ def max_over_ranks(x, pg, device="cpu"):
     return float(t.item())
 
 
+def cpu_baseline_leg(raw, tab, min_s=10.0):
+    """The oracle's float32 iteration (scipy.fft, all host cores) on a bounded
+    sample of the workload's deskewed volume."""
+    cores = os.cpu_count() or 1
+    X, H = cpu_prepare(raw, tab)
+    cpu_time_iterations(X, H, 1, cores)  # warm-up (FFT plans, page faults)
+    v, dt, n = cpu_time_bounded(X, H, cores, min_s=min_s)
+    return {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+            "sample": f"{n} RL iterations (runs of 5 of the {WORKLOAD['n_iters']}) on the deskewed "
+                      f"{X.size}-voxel volume (scipy.fft float32, {cores} threads), {dt:.1f} s"}
+
+
+def reference_gpu_available():
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return False, "no CUDA device"
+        from oracle import ref_kernels as RK
+        return RK.available()
+    except Exception as e:  # noqa: BLE001 - reported in the JSON line
+        return False, f"{type(e).__name__}: {e}"
+
+
 def run_reference(args):
+    """The reference's own implementation of the path.  Its RL loop exists only
+    on the GPU (its kernels with cuFFT, src/RL-Biggs-Andrews.cpp:56-450); the
+    reference's CUDA sources are compiled to PTX and launched in the order of
+    its host code by oracle/ref_runner.cu (a replay of one RL_interface call:
+    background subtraction, bleach statistic, deskew, the loop with the
+    per-iteration host round trip for lambda, rotation), on buffers and cuFFT
+    plans made once.  value: device-resident raw stack, CUDA events; e2e: the
+    float stack copied in and the result copied out (pinned buffers) inside
+    the timed region.  Where the reference runner is not built, the timed arm
+    is the CPU restatement (oracle port)."""
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
         if pg:
@@ -214,27 +250,96 @@ def run_reference(args):
         return 0
     with tempfile.TemporaryDirectory() as td:
         raw, tab, _ = make_inputs(td)
-    cores = os.cpu_count() or 1
-    sample_iters = 3
-    X, H = cpu_prepare(raw, tab)
-    nvox = X.size
+    cpu = None if args.no_cpu_baseline else cpu_baseline_leg(raw, tab)
+    ok, why = reference_gpu_available()
+    w = WORKLOAD
+    nz, ny, nx = w["raw_shape"]
+    common = {"impl": "reference", "metric": "RL voxel-iterations/s", "unit": "voxel-iter/s",
+              "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "data": "synthetic (seeded beads + filaments)"}
+    if not ok:
+        if cpu is None:
+            cpu = cpu_baseline_leg(raw, tab)
+        v = cpu["value"]
+        line = dict(common, value=v, ms_per_step=None,
+                    config={"workload": WORKLOAD["name"], "l2_policy": "n/a (CPU)",
+                            "reference_gpu_unavailable": why},
+                    cpu_baseline=cpu,
+                    e2e={"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0})
+        print(json.dumps(line), flush=True)
+        if pg:
+            pg.barrier()
+        return 0
+    import torch
+    from cudadecon_gb300 import synth
+    from oracle import ref_kernels as RK
+    from oracle import rl_oracle as O
+    torch.cuda.set_device(local)
+    st = O.rl_init(nx, ny, nz, w["dr"], w["dz"], w["dr_psf"], w["dz_psf"], w["angle"], w["angle"],
+                   0, False, synth.otf_table_to_image(tab))
+    sess = RK.Session(st)
+    rawf = np.ascontiguousarray(raw[:st.output_nz, :st.output_ny, :st.output_nx], np.float32)
+    d_raw = torch.from_numpy(rawf).cuda()
+    d_out = torch.empty(sess.out_shape, dtype=torch.float32, device="cuda")
+    n_iters = w["n_iters"]
+    bg = w["background"]
     for _ in range(args.warmup):
-        cpu_time_iterations(X, H, 1, cores)
-    vals = [cpu_time_iterations(X, H, sample_iters, cores)[0] for _ in range(args.steps)]
-    v = statistics.median(vals)
-    sample = (f"{sample_iters} of {WORKLOAD['n_iters']} RL iterations per step on the deskewed "
-              f"{nvox}-voxel volume (scipy.fft float32, {cores} threads)")
-    line = {
-        "impl": "reference", "metric": "RL voxel-iterations/s", "value": v,
-        "unit": "voxel-iter/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * nvox * sample_iters / v, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD["name"], "l2_policy": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
-    }
+        sess.step(d_raw, bg, n_iters, d_out)
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)  # nvidia-smi's first row
+    t_wall0 = time.time()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        sess.step(d_raw, bg, n_iters, d_out)
+    e1.record()
+    e1.synchronize()
+    t_wall1 = time.time()
+    clocks = clk.stop(t_wall0, t_wall1)
+    ms = e0.elapsed_time(e1) / args.steps
+    gz, gy, gx = sess.grid
+    vox_iters = gz * gy * gx * n_iters
+    value = vox_iters / (ms * 1e-3)
+    finite = bool(torch.isfinite(d_out).all().item())
+    # per iteration: the same call without iterations, subtracted
+    sess.step(d_raw, bg, 0, d_out)
+    e0.record()
+    for _ in range(args.steps):
+        sess.step(d_raw, bg, 0, d_out)
+    e1.record()
+    e1.synchronize()
+    prepost_ms = e0.elapsed_time(e1) / args.steps
+    iter_ms = (ms - prepost_ms) / n_iters
+    # e2e: float stack in, result out, through pinned host buffers
+    h_raw = torch.from_numpy(rawf).pin_memory()
+    h_out = torch.empty(sess.out_shape, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d_raw.copy_(h_raw)
+        sess.step(d_raw, bg, n_iters, d_out)
+        h_out.copy_(d_out)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    sess.close()
+    line = dict(common, value=value, ms_per_step=ms,
+                config={"workload": WORKLOAD["name"], "decon_grid_zyx": [gz, gy, gx],
+                        "iterations": n_iters, "form": "reference kernels + cuFFT (plain FP32)",
+                        "reference_impl": "src/RLgpuImpl.cu, geometryTransform.cu compiled to PTX "
+                                          "from the reference's sources, launched in the order of "
+                                          "RichardsonLucy_GPU (oracle/ref_runner.cu); buffers and "
+                                          "cuFFT plans made once",
+                        "l2_policy": "working set ~0.5 GB > 129 MB L2 (no flush needed)"},
+                iteration_ms=iter_ms, prepost_ms_per_step=prepost_ms,
+                cpu_baseline=cpu, clocks=clocks, output_finite=finite,
+                e2e={"value": vox_iters / e2e_s, "unit": "voxel-iter/s",
+                     "h2d_bytes_per_step": int(rawf.nbytes),
+                     "d2h_bytes_per_step": int(h_out.numel() * 4)})
     print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
@@ -448,16 +553,30 @@ def run_gb300(args):
     e2e_s = max_over_ranks(e2e_s, pg, dev)
     e2e_val = world * vox_iters / e2e_s
 
+    # ---- the same call with pageable numpy buffers, as a ctypes caller such
+    # as pycudadecon passes them
+    p_raw = np.ascontiguousarray(raw)
+    p_out = np.empty((onz, ony, onx), np.float32)
+    prawp = p_raw.ctypes.data_as(u16p)
+    poutp = p_out.ctypes.data_as(f32p)
+
+    def e2e_pageable_step():
+        ok = L.RL_interface(prawp, nx, ny, nz, poutp, None, w["background"], False, False,
+                            n_iters, 0, 0, 0, 0.0, False, False)
+        if ok != 1:
+            raise RuntimeError(L.cdx_last_error().decode())
+
+    e2e_pageable_step()
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_pageable_step()
+    e2e_pg_s = max_over_ranks((time.perf_counter() - t0) / args.steps, pg, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cores = os.cpu_count() or 1
-        X, H = cpu_prepare(raw, tab)
-        cpu_time_iterations(X, H, 1, cores)  # warm-up (FFT plans, page faults)
-        v, dt, n = cpu_time_bounded(X, H, cores)
-        nvox = X.size
-        cpu = {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
-               "sample": f"{n} RL iterations (runs of 5 of the 15) on the deskewed "
-                         f"{nvox}-voxel volume (scipy.fft float32, {cores} threads), {dt:.1f} s"}
+        cpu = cpu_baseline_leg(raw, tab)
 
     batch = None
     if rank == 0 and not args.no_batch:
@@ -474,7 +593,11 @@ def run_gb300(args):
                        "parallelism": f"replicas x{world}",
                        "l2_policy": "working set ~0.45 GB > 129 MB L2 (no flush needed)"},
             "e2e": {"value": e2e_val, "unit": "voxel-iter/s",
-                    "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": int(h_out.numel() * 4)},
+                    "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": int(h_out.numel() * 4),
+                    "host_buffers": "pinned",
+                    "pageable": {"value": world * vox_iters / e2e_pg_s, "unit": "voxel-iter/s",
+                                 "ms_per_step": 1e3 * e2e_pg_s,
+                                 "host_buffers": "pageable numpy arrays"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic,
                          "nominal_gbs": NOMINAL_HBM_GBS, "frac_of_nominal": achieved / NOMINAL_HBM_GBS,

@@ -99,6 +99,8 @@ def _bind(L) -> None:
         "cdx_profile_read": (c_int, [POINTER(c_double), POINTER(c_longlong), c_int,
                                      POINTER(c_double), POINTER(c_longlong)]),
         "cdx_profile_pass_name": (c_char_p, [c_int]),
+        "cdx_lambda_trace": (c_int, [c_int]),
+        "cdx_lambda_read": (c_int, [_F, c_int]),
         "cdx_deskew_device": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_void_p, c_int,
                                       c_int, c_float, c_void_p]),
         "cdx_rotate_device": (c_int, [c_void_p, c_int, c_int, c_int, _F, c_void_p, c_int, c_int,

@@ -134,6 +134,9 @@ struct Session {
   DevBuf<double> partials, stat_d;
   DevBuf<unsigned> stat_u;
   DevBuf<float> lam;
+  // acceleration factors of the last call, per iteration (cdx_lambda_trace)
+  DevBuf<float> lam_hist;
+  int lam_hist_n = 0;
   cudaStream_t stream = nullptr;
   long long launches = 0;
   // acceleration-factor scratch (per-block partials and the last-block ticket)
@@ -223,6 +226,8 @@ static void release_all(Session& s) {
   s.stat_d.release();
   s.stat_u.release();
   s.lam.release();
+  s.lam_hist.release();
+  s.lam_hist_n = 0;
   s.cc_param.release();
   s.cc_in.release();
   s.cc_out.release();
@@ -367,7 +372,8 @@ struct LoopBufs {
 };
 
 static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t st, bool prof,
-                   float** final_x, long long* launches) {
+                   float** final_x, long long* launches, float* lam_hist = nullptr,
+                   int hist_n = 0) {
   const Geom& g = p.g;
   RLWork w;
   w.partials = b.partials;
@@ -410,6 +416,10 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
     if ((rc = launch_x_inv_update(g, p.fx, b.S, Y, Xm1, b.G, k >= 1, w, lam_n, eps, st)))
       return rc;
     mark();
+    // trace: the factor iteration k+1 uses (computed from G_k and G_{k-1})
+    if (lam_hist && k >= 1 && k + 1 < hist_n)
+      CDX_CHECK(cudaMemcpyAsync(lam_hist + k + 1, lam_n, sizeof(float), cudaMemcpyDeviceToDevice,
+                                st));
     if (prof && g_prof.used >= 10 * 64) prof_collect();
     *launches += k >= 1 ? 10 : 9;  // the update pass adds the lambda kernel
     float* t = X;
@@ -423,7 +433,13 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
 static int rl_iterations(Session& s, int nIter, float** final_x) {
   const LoopBufs b{s.Xa.p, s.Xb.p, s.G.p, s.raw.p, s.S.p, s.partials.p, s.lam.p,
                    (int)(s.partials.n / 2)};
-  return rl_loop(s.plan, b, nIter, s.stream, g_prof.on, final_x, &s.launches);
+  float* hist = nullptr;
+  if (s.lam_hist_n > 0 && s.lam_hist.p) {
+    CDX_CHECK(cudaMemsetAsync(s.lam_hist.p, 0, sizeof(float) * s.lam_hist_n, s.stream));
+    hist = s.lam_hist.p;
+  }
+  return rl_loop(s.plan, b, nIter, s.stream, g_prof.on, final_x, &s.launches, hist,
+                 s.lam_hist_n);
 }
 
 struct RLArgs {
@@ -1099,6 +1115,37 @@ int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, dou
 }
 
 const char* cdx_profile_pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : ""; }
+
+int cdx_lambda_trace(int n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (n <= 0) {
+    s.lam_hist.release();
+    s.lam_hist_n = 0;
+    return 1;
+  }
+  if (s.lam_hist.ensure((size_t)n)) return 0;
+  s.lam_hist_n = n;
+  return 1;
+}
+
+int cdx_lambda_read(float* out, int n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!out || s.lam_hist_n <= 0 || !s.lam_hist.p) {
+    set_error("cdx_lambda_read", "no trace enabled (cdx_lambda_trace)");
+    return -1;
+  }
+  const int m = n < s.lam_hist_n ? n : s.lam_hist_n;
+  cudaError_t e = cudaStreamSynchronize(s.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(out, s.lam_hist.p, sizeof(float) * (size_t)m, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_cuda_error("cdx_lambda_read", e);
+    return -1;
+  }
+  return m;
+}
 
 void RL_cleanup(void) {
   std::lock_guard<std::mutex> lk(g_mu);

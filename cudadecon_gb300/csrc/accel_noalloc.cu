@@ -33,12 +33,54 @@ constexpr long long kNoAllocMaxElems = (long long)kNoAllocMaxBlocks * kDotElemsP
 // final element (used as an unsigned).
 static __device__ __align__(256) double g_accel_scratch[2 * kNoAllocMaxBlocks + 1];
 
-// Device address of g_accel_scratch per device ordinal.  In host code the
-// name g_accel_scratch is only a host-side stand-in, so the address is asked
-// from the runtime once per device, with that device current.
+// Device address of g_accel_scratch, looked up once per device and context.
+// In host code the name g_accel_scratch is only a host-side stand-in, so the
+// address is asked from the runtime (cudaGetSymbolAddress) with the device
+// current.  The array lives in the context's copy of the module: after
+// cudaDeviceReset (cuda_reset) or under another context of the same device
+// it may sit at another address, so each cached address is tagged with the
+// id of the context it was looked up in and looked up again when the
+// current context's id differs.  The context id comes from the driver
+// (cuCtxGetCurrent, cuCtxGetId), reached through the runtime's entry-point
+// query so that the library does not link libcuda.
 constexpr int kMaxDevices = 64;
-static double* g_scratch_addr[kMaxDevices] = {nullptr};
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  double* addr = nullptr;
+};
+static ScratchAddr g_scratch_addr[kMaxDevices];
 static std::mutex g_scratch_mu;
+
+typedef int (*PfnCtxGetCurrent)(void** ctx);
+typedef int (*PfnCtxGetId)(void* ctx, unsigned long long* id);
+static PfnCtxGetCurrent g_ctx_get_current = nullptr;
+static PfnCtxGetId g_ctx_get_id = nullptr;
+static bool g_ctx_fns_queried = false;
+
+// Id of the current context (0 when there is none or the driver cannot say).
+static unsigned long long current_context_id() {
+  if (!g_ctx_fns_queried) {
+    g_ctx_fns_queried = true;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) ==
+            cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) ==
+            cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+      g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f2);
+    }
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != 0 || !ctx) return 0;
+  if (g_ctx_get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 static int scratch_for_current_device(double** out) {
   int dev = 0;
@@ -52,16 +94,22 @@ static int scratch_for_current_device(double** out) {
     return cudaErrorInvalidDevice;
   }
   std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  const unsigned long long id = current_context_id();
+  ScratchAddr& c = g_scratch_addr[dev];
+  // id 0: no context yet (the lookup below creates the primary context) or
+  // no driver answer; then the address is looked up on every call
+  if (!c.addr || id == 0 || c.ctx_id != id) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_accel_scratch);
     if (e != cudaSuccess || !p) {
       set_cuda_error("cdx_accel_factor_device_noalloc: cudaGetSymbolAddress", e);
+      c = ScratchAddr{};
       return e != cudaSuccess ? e : cudaErrorInvalidSymbol;
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    c.addr = static_cast<double*>(p);
+    c.ctx_id = id ? id : current_context_id();
   }
-  *out = g_scratch_addr[dev];
+  *out = c.addr;
   return 0;
 }
 

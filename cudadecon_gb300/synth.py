@@ -173,6 +173,33 @@ def bead_stack(shape, n_beads=200, sigma_range=(0.5, 2.0), amp_range=(500.0, 500
     return np.clip(np.rint(img), 0, 65535).astype(np.uint16)
 
 
+def bead_stack_gpu(shape, n_beads=2000, amp_range=(500.0, 5000.0), psf_sigma_xy=1.5,
+                   psf_sigma_z=4.0, background=100.0, seed=1001, device="cuda"):
+    """Large stacks generated on the GPU (seeded torch generator): point
+    beads of uniform amplitude, blurred by the Gaussian PSF (FFT on the
+    device), plus background and Poisson noise.  Returns a (nz, ny, nx)
+    uint16 tensor on `device`."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    nz, ny, nx = (int(v) for v in shape)
+    obj = torch.zeros((nz, ny, nx), dtype=torch.float32, device=device)
+    idx = torch.randint(0, nz * ny * nx, (n_beads,), generator=gen, device=device)
+    amp = amp_range[0] + (amp_range[1] - amp_range[0]) * torch.rand(
+        n_beads, generator=gen, device=device)
+    obj.view(-1).index_add_(0, idx, amp * (2 * np.pi) ** 1.5 * psf_sigma_xy ** 2 * psf_sigma_z)
+    fz = torch.fft.fftfreq(nz, device=device)[:, None, None]
+    fy = torch.fft.fftfreq(ny, device=device)[None, :, None]
+    fx = torch.fft.rfftfreq(nx, device=device)[None, None, :]
+    otf = torch.exp(-2 * np.pi ** 2 * ((psf_sigma_z * fz) ** 2 + (psf_sigma_xy * fy) ** 2 +
+                                       (psf_sigma_xy * fx) ** 2))
+    img = torch.fft.irfftn(torch.fft.rfftn(obj) * otf, s=(nz, ny, nx))
+    del obj, otf
+    img = img.clamp_(min=0.0).add_(background)
+    img = torch.poisson(img, generator=gen)
+    return img.clamp_(0, 65535).to(torch.int32).to(torch.uint16)
+
+
 def camcor_params(ny, nx, seed=1005, offset=(90.0, 110.0), coeff=(0.0, 0.02)) -> np.ndarray:
     """(3, ny, nx) float32 sCMOS parameters: planes a, b, offset."""
     rng = np.random.default_rng(seed)

@@ -133,6 +133,15 @@ int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, dou
                      long long* iter_count);
 const char* cdx_profile_pass_name(int i);
 
+/* Trace of the Biggs-Andrews acceleration factors (extension; the reference
+ * prints them, RL-Biggs-Andrews.cpp:300).  cdx_lambda_trace(n) with n > 0
+ * makes every later RL call record, for iteration k < n, the factor lambda_k
+ * it applied (0 for k <= 1, which predict nothing); n == 0 stops tracing.
+ * cdx_lambda_read waits for the last call and copies min(n, traced) factors
+ * to out; it returns their number, or -1 without a trace. */
+int cdx_lambda_trace(int n);
+int cdx_lambda_read(float* out, int n);
+
 /* Deskew / rotate / camcor on device pointers (same arithmetic as the
  * reference kernels).  rot is a host pointer to the 4 rotation-matrix floats. */
 int cdx_deskew_device(const float* in, int nx, int ny, int nz, double deskewFactor, float* out,
@@ -170,7 +179,9 @@ int cdx_accel_factor_device(const float* g_new, const float* g_old, long long n,
  * loads the library; n is limited to 33554432 elements (larger n returns 0
  * with an error message).  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current, so make it
- * before any stream capture.  All calls share the array and clear its counter
+ * before any stream capture; the lookup is repeated when the current context
+ * is another one than at the last lookup (after cuda_reset, or under a
+ * context the caller made).  All calls share the array and clear its counter
  * on entry: calls that may overlap on the GPU race and must be serialised. */
 int cdx_accel_factor_device_noalloc(const float* g_new, const float* g_old, long long n,
                                     double* out, float* lam, void* stream);

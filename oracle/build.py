@@ -4,9 +4,10 @@
   the compiler adds no fused multiply-adds beyond the explicit fma() calls;
   gcc on aarch64 would otherwise contract).
 * The reference's own CUDA kernels, compiled from its sources where they lie
-  (/root/reference/src/{RLgpuImpl,geometryTransform,camcor}.cu, with its
-  Buffers/ headers) to PTX in oracle/_ref/ — only where the reference is
-  present.  The PTX travels with the repository to the GPU machine, where
+  (src/{RLgpuImpl,geometryTransform,camcor}.cu of the reference checkout, with
+  its Buffers/ headers) to PTX in oracle/_ref/ — only where the reference is
+  present.  The checkout is taken from the CDX_REFERENCE_DIR environment
+  variable or the --reference argument, by default /root/reference.  The PTX travels with the repository to the GPU machine, where
   ref_runner.cu (our launcher, driver API + cuFFT) is compiled against it into
   oracle/_ref/libref_runner.so.  Nothing here reads the PTX; it is loaded with
   cuModuleLoad.
@@ -14,6 +15,8 @@
 
 from __future__ import annotations
 
+import argparse
+import os
 import subprocess
 from pathlib import Path
 
@@ -33,7 +36,7 @@ def build_geom() -> Path:
     return out
 
 
-REF_SRC = Path("/root/reference/src")
+REF_SRC = Path(os.environ.get("CDX_REFERENCE_DIR", "/root/reference")) / "src"
 REF_OUT = HERE / "_ref"
 REF_UNITS = ["RLgpuImpl", "geometryTransform", "camcor"]
 
@@ -84,5 +87,10 @@ def build_all() -> None:
 
 
 if __name__ == "__main__":
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", help="reference checkout (its src/ holds the .cu sources)")
+    a = ap.parse_args()
+    if a.reference:
+        REF_SRC = Path(a.reference) / "src"
     build_all()
     print("ok")

@@ -50,6 +50,12 @@ def _load():
     L.ref_rl_iterations.argtypes = [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp,
                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                     ctypes.c_float, ctypes.c_float, ctypes.c_int, _dp]
+    L.ref_session_open.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_int, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_float, _fp,
+                                   ctypes.c_int, ctypes.c_int]
+    L.ref_session_step.argtypes = [_vp, ctypes.c_float, ctypes.c_int, _vp]
+    L.ref_session_close.restype = None
     if L.ref_load(str(REF).encode()) != 1:
         _why = "ref_load failed: " + L.ref_last_error().decode()
         return None
@@ -134,3 +140,54 @@ def rl_iterations(X0, raw, otf_complex, kscales, n_iters):
                                      float(kscales[2]), int(n_iters), lam.ctypes.data_as(_dp)),
            "ref_rl_iterations")
     return X.cpu().numpy(), lam[:n_iters]
+
+
+class Session:
+    """One RL_interface call's device work with the reference's kernels and
+    cuFFT (RichardsonLucy_GPU, src/RL-Biggs-Andrews.cpp:56-450): background
+    subtraction, the bleach statistic, deskew, the RL loop with its
+    per-iteration host round trip for lambda, rotation.  `state` is the
+    oracle's restatement of RL_interface_init (oracle.rl_oracle.rl_init);
+    buffers and cuFFT plans are made once here, as the plans are in
+    RL_interface_init.  step() takes the cropped stack as a float32 device
+    tensor (the reference converts u16 to float on the host) and writes the
+    result into a device tensor of out_shape."""
+
+    def __init__(self, state):
+        from oracle import rl_oracle as O
+        L = _load()
+        if L is None:
+            raise RuntimeError(_why)
+        nz, ny, nx = state.output_nz, state.output_ny, state.output_nx
+        desk = abs(state.deskewFactor) > 0.0
+        gx = state.deskewedXdim if desk else nx
+        kxs, kys, kzs = O.kscales(state, gx, ny, nz)
+        otf = np.ascontiguousarray(state.otf, np.complex64)
+        if otf.ndim == 2:
+            nxo, nyo, nzo = otf.shape[0], 1, otf.shape[1]
+        else:
+            nzo, nyo, nxo = otf.shape
+        self._otf = otf.view(np.float32).reshape(-1)
+        rot = None
+        nxr, nzr = gx, nz
+        if state.rot is not None:
+            rot = np.ascontiguousarray(state.rot, np.float32)
+            nxr, nzr = O.rotated_dims(gx, nz, rot)
+        self._rot = rot
+        self.raw_shape = (nz, ny, nx)
+        self.grid = (nz, ny, gx)
+        self.out_shape = (nzr, ny, nxr)
+        _check(L.ref_session_open(nx, ny, nz, float(state.deskewFactor), int(gx),
+                                  self._otf.ctypes.data_as(_fp), nxo, nyo, nzo, float(kxs),
+                                  float(kys), float(kzs),
+                                  rot.ctypes.data_as(_fp) if rot is not None else None,
+                                  int(nxr), int(nzr)), "ref_session_open")
+
+    def step(self, d_raw, background, n_iters, d_out):
+        _check(_load().ref_session_step(d_raw.data_ptr(), float(background), int(n_iters),
+                                        d_out.data_ptr()), "ref_session_step")
+
+    def close(self):
+        L = _load()
+        if L is not None:
+            L.ref_session_close()

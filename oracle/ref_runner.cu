@@ -16,6 +16,12 @@
 //   ref_deskew / ref_rotate <- deskew_GPU / rotate_GPU (geometryTransform.cu:33-48, 90-106)
 //   ref_camcor         <- setupCamCor / setupData / camcor_GPU (camcor.cu:6-122)
 //   ref_affine         <- affine_GPU / affine_GPU_RA (geometryTransform.cu:257-349)
+//   ref_session_open / ref_session_step / ref_session_close
+//                      <- one RL_interface call's device work
+//                         (RichardsonLucy_GPU, src/RL-Biggs-Andrews.cpp:56-450:
+//                         background subtraction, the bleach statistic,
+//                         deskew, the loop, rotate) on buffers and cuFFT plans
+//                         made once, as RL_interface_init makes the plans
 // Every entry point returns 1 on success, 0 on failure.
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -352,6 +358,236 @@ int ref_rl_iterations(float* X, const float* raw, int nx, int ny, int nz, const 
   cudaFree(G2);
   cudaFree(d_part);
   return ok ? 1 : 0;
+}
+
+
+// ---------------------------------------------------------------- session
+// One RL_interface call's device work, for timing the reference's own GPU
+// path: buffers and plans are made once (the reference allocates its
+// buffers on every call, RL-Biggs-Andrews.cpp:92-96, 211-260, which this
+// leaves out in the reference's favour).
+namespace {
+struct RefSession {
+  bool open = false;
+  int nx_raw = 0, ny = 0, nz = 0, nx = 0;  // raw grid and deskewed (decon) width
+  double deskew = 0.0;
+  int nx_rot = 0, nz_rot = 0;
+  size_t N = 0, M = 0, Nraw = 0;
+  float2 *rawotf = nullptr, *otf = nullptr, *fft = nullptr;
+  float *X0 = nullptr, *X = nullptr, *CC = nullptr, *rawb = nullptr, *Xm1 = nullptr, *Y = nullptr;
+  float *G1 = nullptr, *G2 = nullptr, *rot = nullptr;
+  double* part = nullptr;
+  double* intres = nullptr;
+  unsigned* counter = nullptr;
+  unsigned nbDot = 0, nbSum = 0;
+  cufftHandle pf = 0, pi = 0;
+  std::vector<double> hpart, hsum;
+  std::vector<unsigned> hcnt;
+};
+RefSession g_s;
+
+void session_free() {
+  if (g_s.pf) cufftDestroy(g_s.pf);
+  if (g_s.pi) cufftDestroy(g_s.pi);
+  void* bufs[] = {g_s.rawotf, g_s.otf, g_s.fft, g_s.X0,   g_s.X,      g_s.CC,      g_s.rawb,
+                  g_s.Xm1,    g_s.Y,   g_s.G1,  g_s.G2,   g_s.rot,    g_s.part,    g_s.intres,
+                  g_s.counter};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  g_s = RefSession{};
+}
+}  // namespace
+
+void ref_session_close(void) { session_free(); }
+
+// nx_raw, ny, nz: the cropped raw grid; deskewFactor / nx_desk as
+// RL_interface_init computes them (nx_desk = nx_raw when deskewFactor is 0);
+// rot4: the rotation matrix, or NULL for no rotation (then nx_rot, nz_rot
+// are ignored).
+int ref_session_open(int nx_raw, int ny, int nz, double deskewFactor, int nx_desk,
+                     const float* otf_host, int nxotf, int nyotf, int nzotf, float kxs, float kys,
+                     float kzs, const float* rot4, int nx_rot, int nz_rot) {
+  session_free();
+  RefSession& s = g_s;
+  s.nx_raw = nx_raw;
+  s.ny = ny;
+  s.nz = nz;
+  s.deskew = deskewFactor;
+  s.nx = fabs(deskewFactor) > 0.0 ? nx_desk : nx_raw;
+  s.nx_rot = rot4 ? nx_rot : 0;
+  s.nz_rot = rot4 ? nz_rot : 0;
+  s.N = (size_t)s.nx * ny * nz;
+  s.M = (size_t)nz * ny * (s.nx / 2 + 1);
+  s.Nraw = (size_t)nx_raw * ny * nz;
+  const int nx = s.nx;
+  const float eps = std::numeric_limits<float>::epsilon();
+  unsigned nxyz = (unsigned)s.N;
+  if (!set_const("const_nx", &nx, 4) || !set_const("const_ny", &ny, 4) ||
+      !set_const("const_nz", &nz, 4) || !set_const("const_nxyz", &nxyz, 4) ||
+      !set_const("const_nxotf", &nxotf, 4) || !set_const("const_nyotf", &nyotf, 4) ||
+      !set_const("const_nzotf", &nzotf, 4) || !set_const("const_kxscale", &kxs, 4) ||
+      !set_const("const_kyscale", &kys, 4) || !set_const("const_kzscale", &kzs, 4) ||
+      !set_const("const_eps", &eps, 4))
+    return 0;
+  const size_t notf = (size_t)nxotf * nyotf * nzotf;
+  s.nbDot = (unsigned)ceil(((float)s.N) / 1024 / 2);
+  s.nbSum = (unsigned)ceil(s.Nraw / (float)1024 / 2);
+  bool ok = ok_rt(cudaMalloc(&s.rawotf, notf * sizeof(float2)), "malloc") &&
+            ok_rt(cudaMalloc(&s.otf, s.M * sizeof(float2)), "malloc") &&
+            ok_rt(cudaMalloc(&s.fft, s.M * sizeof(float2)), "malloc") &&
+            ok_rt(cudaMalloc(&s.X0, s.Nraw * 4), "malloc") &&
+            ok_rt(cudaMalloc(&s.X, s.N * 4), "malloc") && ok_rt(cudaMalloc(&s.CC, s.N * 4), "malloc") &&
+            ok_rt(cudaMalloc(&s.rawb, s.N * 4), "malloc") &&
+            ok_rt(cudaMalloc(&s.Xm1, s.N * 4), "malloc") && ok_rt(cudaMalloc(&s.Y, s.N * 4), "malloc") &&
+            ok_rt(cudaMalloc(&s.G1, s.N * 4), "malloc") && ok_rt(cudaMalloc(&s.G2, s.N * 4), "malloc") &&
+            ok_rt(cudaMalloc(&s.part, 2 * s.nbDot * sizeof(double)), "malloc") &&
+            ok_rt(cudaMalloc(&s.intres, s.nbSum * sizeof(double)), "malloc") &&
+            ok_rt(cudaMalloc(&s.counter, s.nbSum * sizeof(unsigned)), "malloc") &&
+            (!rot4 || ok_rt(cudaMalloc(&s.rot, 4 * sizeof(float)), "malloc"));
+  if (ok && rot4) ok = ok_rt(cudaMemcpy(s.rot, rot4, 16, cudaMemcpyHostToDevice), "rot");
+  if (ok) {
+    ok = ok_rt(cudaMemcpy(s.rawotf, otf_host, notf * sizeof(float2), cudaMemcpyHostToDevice),
+               "otf");
+    void* a_otf[] = {&s.rawotf, &s.otf};
+    unsigned bnx = (unsigned)ceil((nx / 2 + 1) / (float)128);
+    ok = ok && launch(fn(g_rl, "_Z19makeOTFarray_kernelP6float2S0_"), dim3(bnx, ny, nz),
+                      dim3(128), 0, a_otf);
+    ok = ok && cufftPlan3d(&s.pf, nz, ny, nx, CUFFT_R2C) == CUFFT_SUCCESS &&
+         cufftPlan3d(&s.pi, nz, ny, nx, CUFFT_C2R) == CUFFT_SUCCESS;
+    if (!ok && g_err.empty()) g_err = "cufftPlan3d failed";
+  }
+  ok = ok && ok_rt(cudaDeviceSynchronize(), "sync");
+  s.hpart.resize(2 * s.nbDot);
+  s.hsum.resize(s.nbSum);
+  s.hcnt.resize(s.nbSum);
+  if (!ok) {
+    session_free();
+    return 0;
+  }
+  s.open = true;
+  return 1;
+}
+
+// One call: raw (device, the cropped (nz, ny, nx_raw) stack as float, which
+// the reference converts on the host) -> out (device, the rotated result, or
+// the deskewed decon grid without rotation).  Returns after the device work.
+int ref_session_step(const float* d_raw, float background, int nIter, float* d_out) {
+  RefSession& s = g_s;
+  if (!s.open) {
+    g_err = "session not open";
+    return 0;
+  }
+  const size_t N = s.N, M = s.M;
+  const float eps = std::numeric_limits<float>::epsilon();
+  // X_k <- raw (the reference's H2D), backgroundSubtraction_GPU (RLgpuImpl.cu:134-154)
+  bool ok = ok_rt(cudaMemcpyAsync(s.X0, d_raw, s.Nraw * 4, cudaMemcpyDeviceToDevice), "copy");
+  {
+    size_t n = s.Nraw;
+    void* a[] = {&s.X0, &n, &background};
+    ok = ok && launch(fn(g_rl, "_Z14bgsubtr_kernelPfmf"), grid1024(s.Nraw), dim3(1024), 0, a);
+  }
+  // meanAboveBackground_GPU (RLgpuImpl.cu:668-718): computed on every call
+  if (ok) {
+    int n = (int)s.Nraw;
+    void* a1[] = {&s.X0, &s.intres, &n};
+    ok = launch(fn(g_rl, "_Z16summation_kernelPfPdi"), dim3(s.nbSum), dim3(1024),
+                1024 * sizeof(double), a1) &&
+         ok_rt(cudaMemcpy(s.hsum.data(), s.intres, s.nbSum * sizeof(double),
+                          cudaMemcpyDeviceToHost),
+               "sum");
+    double sum = 0;
+    for (double v : s.hsum) sum += v;
+    float mean = (float)(sum / (double)s.Nraw);
+    void* a2[] = {&s.X0, &s.intres, &s.counter, &mean, &n};
+    ok = ok &&
+         launch(fn(g_rl, "_Z21sumAboveThresh_kernelPfPdPjfi"), dim3(s.nbSum), dim3(1024),
+                1024 * (sizeof(double) + sizeof(unsigned)), a2) &&
+         ok_rt(cudaMemcpy(s.hcnt.data(), s.counter, s.nbSum * sizeof(unsigned),
+                          cudaMemcpyDeviceToHost),
+               "count") &&
+         ok_rt(cudaMemcpy(s.hsum.data(), s.intres, s.nbSum * sizeof(double),
+                          cudaMemcpyDeviceToHost),
+               "sum");
+  }
+  // deskew_GPU (geometryTransform.cu:33-48) into the decon grid
+  if (ok && fabs(s.deskew) > 0.0) {
+    int nxr = s.nx_raw, ny = s.ny, nz = s.nz, nxo = s.nx, shift = 0;
+    double f = s.deskew;
+    float pad = 0.f;
+    void* a[] = {&s.X0, &nxr, &ny, &nz, &s.X, &nxo, &shift, &f, &pad};
+    unsigned nxb = (unsigned)ceil(nxo / (float)128);
+    ok = launch(fn(g_geo, "_Z13deskew_kernelPfiiiS_iidf"), dim3(nxb, ny, nz), dim3(128), 0, a);
+  } else if (ok) {
+    ok = ok_rt(cudaMemcpyAsync(s.X, s.X0, N * 4, cudaMemcpyDeviceToDevice), "copy");
+  }
+  ok = ok && ok_rt(cudaMemcpyAsync(s.rawb, s.X, N * 4, cudaMemcpyDeviceToDevice), "copy");
+  CUfunction f_scale = fn(g_rl, "_Z12scale_kernelPfd");
+  CUfunction f_filt = fn(g_rl, "_Z13filter_kernelP6float2S0_i");
+  CUfunction f_filtc = fn(g_rl, "_Z17filterConj_kernelP6float2S0_i");
+  CUfunction f_lr = fn(g_rl, "_Z13LRcore_kernelPfS_");
+  CUfunction f_est = fn(g_rl, "_Z19currEstimate_kernelPfS_S_");
+  CUfunction f_diff = fn(g_rl, "_Z19currPrevDiff_kernelPfS_S_");
+  CUfunction f_dot = fn(g_rl, "_Z19innerProduct_kernelPfS_Pd");
+  CUfunction f_pred = fn(g_rl, "_Z23updatePrediction_kernelPfS_S_f");
+  auto filter = [&](bool conj) -> bool {
+    double factor = 1. / (double)N;
+    void* a1[] = {&s.CC, &factor};
+    if (!launch(f_scale, grid1024(N), dim3(1024), 0, a1)) return false;
+    if (cufftExecR2C(s.pf, s.CC, (cufftComplex*)s.fft) != CUFFT_SUCCESS) {
+      g_err = "cufftExecR2C";
+      return false;
+    }
+    int msz = (int)M;
+    void* a2[] = {&s.fft, &s.otf, &msz};
+    if (!launch(conj ? f_filtc : f_filt, grid1024(M), dim3(1024), 0, a2)) return false;
+    if (cufftExecC2R(s.pi, (cufftComplex*)s.fft, s.CC) != CUFFT_SUCCESS) {
+      g_err = "cufftExecC2R";
+      return false;
+    }
+    return true;
+  };
+  for (int k = 0; ok && k < nIter; ++k) {
+    if (k > 1) {
+      void* a[] = {&s.G1, &s.G2, &s.part};
+      ok = launch(f_dot, dim3(s.nbDot), dim3(1024), 1024 * sizeof(double) * 2, a) &&
+           ok_rt(cudaMemcpy(s.hpart.data(), s.part, s.hpart.size() * sizeof(double),
+                            cudaMemcpyDeviceToHost),
+                 "partials");
+      if (!ok) break;
+      double num = 0, den = 0;
+      for (unsigned i = 0; i < s.nbDot; ++i) {
+        num += s.hpart[i];
+        den += s.hpart[i + s.nbDot];
+      }
+      double lambda = num / (den + eps);
+      lambda = std::max(std::min(lambda, 1.), 0.);
+      float lf = (float)lambda;
+      void* ap[] = {&s.Y, &s.X, &s.Xm1, &lf};
+      ok = launch(f_pred, grid1024(N), dim3(1024), 0, ap);
+    } else {
+      ok = ok_rt(cudaMemcpyAsync(s.Y, s.X, N * 4, cudaMemcpyDeviceToDevice), "copy");
+    }
+    ok = ok && ok_rt(cudaMemcpyAsync(s.Xm1, s.X, N * 4, cudaMemcpyDeviceToDevice), "copy");
+    if (ok && k > 0) ok = ok_rt(cudaMemcpyAsync(s.G2, s.G1, N * 4, cudaMemcpyDeviceToDevice), "copy");
+    ok = ok && ok_rt(cudaMemcpyAsync(s.CC, s.Y, N * 4, cudaMemcpyDeviceToDevice), "copy") &&
+         filter(false);
+    void* alr[] = {&s.CC, &s.rawb};
+    ok = ok && launch(f_lr, grid1024(N), dim3(1024), 0, alr) && filter(true);
+    void* ae[] = {&s.X, &s.CC, &s.Y};
+    ok = ok && launch(f_est, grid1024(N), dim3(1024), 0, ae);
+    void* ad[] = {&s.X, &s.Y, &s.G1};
+    ok = ok && launch(f_diff, grid1024(N), dim3(1024), 0, ad);
+  }
+  // rotate_GPU (geometryTransform.cu:90-106)
+  if (ok && s.rot) {
+    int nx = s.nx, ny = s.ny, nz = s.nz, nxo = s.nx_rot, nzo = s.nz_rot;
+    void* a[] = {&s.X, &nx, &ny, &nz, &d_out, &nxo, &nzo, &s.rot};
+    unsigned nxb = (unsigned)ceil(nxo / (float)128);
+    ok = launch(fn(g_geo, "_Z13rotate_kernelPfiiiS_iiS_"), dim3(nxb, ny, nzo), dim3(128), 0, a);
+  } else if (ok) {
+    ok = ok_rt(cudaMemcpyAsync(d_out, s.X, N * 4, cudaMemcpyDeviceToDevice), "copy");
+  }
+  return ok && ok_rt(cudaDeviceSynchronize(), "sync") ? 1 : 0;
 }
 
 }  // extern "C"

@@ -151,3 +151,24 @@ def test_zblend_oracle_reference_slice_bug(oracle):
     # only slices 1 and nz-2 change, three times each
     assert np.all(out[[0, 2, 3]] == 0)
     np.testing.assert_allclose(out[1], 3 * np.float32(10.0 * w), rtol=1e-6)
+
+
+def test_torch_fp64_oracle_matches_numpy_fp64(oracle):
+    """The torch restatement of the FP64 oracle (used on the GPU for the
+    full-size grids) against the numpy one, on the CPU: OTF grid, estimates
+    and acceleration factors agree to float64 rounding."""
+    torch = pytest.importorskip("torch")
+    from oracle import rl_oracle_torch as OT
+    shape = (12, 20, 30)
+    tab = synth.gaussian_otf_table(17, 10, 1.3, 2.0)
+    st = _state(oracle, shape, tab, dr=0.104, dz=0.3, dr_psf=0.09, dz_psf=0.2)
+    H = oracle.otf_on_grid(st, 30, 20, 12, dtype=np.float64)
+    Ht = OT.otf_on_grid(st, 30, 20, 12, device="cpu")
+    assert rel_l2(Ht.numpy(), H) < 1e-14
+    rng = np.random.default_rng(9)
+    raw = (rng.gamma(2.0, 50.0, shape) + 1.0).astype(np.float32)
+    la, lb = [], []
+    a = oracle.rl_iterations(raw, raw, H, 8, dtype=np.float64, lambdas=la)
+    b = OT.rl_iterations(raw, raw, Ht, 8, lambdas=lb, device="cpu").numpy()
+    assert rel_l2(b, a) < 1e-12
+    assert np.allclose(la, lb, rtol=0, atol=1e-12)

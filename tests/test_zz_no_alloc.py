@@ -11,6 +11,9 @@ This file is collected last on purpose: it must pass both alone in a fresh
 process and after the other tests."""
 
 import ctypes
+import subprocess
+import sys
+import textwrap
 
 import numpy as np
 import pytest
@@ -65,3 +68,80 @@ def test_noalloc_rejects_arrays_beyond_its_scratch(cdx, torch_cuda):
     ok, _, _ = _call(torch, noalloc, d, d, MAX_ELEMS + 1)
     assert ok == 0
     assert b"33554432" in cdx.lib().cdx_last_error()
+
+
+def test_noalloc_at_its_limit_against_float64_sums(cdx, torch_cuda):
+    """n at the limit fills every partial slot of the fixed array; the result
+    is checked against float products summed in float64 (the reference's
+    innerProduct arithmetic, RLgpuImpl.cu:584-592), not only against the
+    allocating entry point, which shares the block code."""
+    torch = torch_cuda
+    L = cdx.lib()
+    noalloc = _bind(L)
+    rng = np.random.default_rng(77)
+    n = MAX_ELEMS
+    g1 = rng.standard_normal(n, dtype=np.float32)
+    g2 = (0.3 * g1 + rng.standard_normal(n, dtype=np.float32)).astype(np.float32)
+    num = float(np.sum(g1 * g2, dtype=np.float64))
+    den = float(np.sum(g2 * g2, dtype=np.float64))
+    d1 = torch.from_numpy(g1).cuda()
+    d2 = torch.from_numpy(g2).cuda()
+    for _ in range(2):
+        ok, got, lam = _call(torch, noalloc, d1, d2, n)
+        assert ok == 1, L.cdx_last_error()
+        np.testing.assert_allclose(got[:2], [num, den], rtol=1e-11)
+        ref_lam = min(max(num / (den + 1.1920928955078125e-07), 0.0), 1.0)
+        assert abs(lam - ref_lam) <= 1e-6
+
+
+_RESET_SCRIPT = textwrap.dedent("""
+    import ctypes, sys
+    import numpy as np
+    L = ctypes.CDLL(sys.argv[1])
+    rt = ctypes.CDLL("libcudart.so.13")
+    vp = ctypes.c_void_p
+    for f in ("cdx_accel_factor_device", "cdx_accel_factor_device_noalloc"):
+        getattr(L, f).restype = ctypes.c_int
+        getattr(L, f).argtypes = [vp, vp, ctypes.c_longlong, vp, vp, vp]
+    L.cdx_last_error.restype = ctypes.c_char_p
+    n = 3000017
+    rng = np.random.default_rng(5)
+    g1 = rng.standard_normal(n).astype(np.float32)
+    g2 = (0.5 * g1 + rng.standard_normal(n)).astype(np.float32)
+
+    def dev_copy(a):
+        p = vp()
+        assert rt.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(a.nbytes)) == 0
+        assert rt.cudaMemcpy(p, a.ctypes.data_as(vp), ctypes.c_size_t(a.nbytes), 1) == 0
+        return p
+
+    def run(fn):
+        d1, d2 = dev_copy(g1), dev_copy(g2)
+        out = dev_copy(np.zeros(3, np.float64))
+        lam = dev_copy(np.zeros(1, np.float32))
+        assert getattr(L, fn)(d1, d2, n, out, lam, None) == 1, L.cdx_last_error()
+        assert rt.cudaDeviceSynchronize() == 0
+        h = np.zeros(3, np.float64)
+        assert rt.cudaMemcpy(h.ctypes.data_as(vp), out, ctypes.c_size_t(24), 2) == 0
+        for q in (d1, d2, out, lam):
+            rt.cudaFree(q)
+        return h
+
+    ref = run("cdx_accel_factor_device")
+    first = run("cdx_accel_factor_device_noalloc")
+    L.cuda_reset()  # new primary context: the array may move
+    second = run("cdx_accel_factor_device_noalloc")
+    third = run("cdx_accel_factor_device_noalloc")
+    for h in (first, second, third):
+        assert np.allclose(h[:2], ref[:2], rtol=1e-12, atol=0), (h, ref)
+    print("ok")
+""")
+
+
+def test_noalloc_after_cuda_reset_in_fresh_process(cdx, torch_cuda):
+    """cuda_reset destroys the primary context; the next call must look the
+    array's address up again in the new context.  Run in a child process so
+    that the reset does not touch this process's CUDA state."""
+    r = subprocess.run([sys.executable, "-c", _RESET_SCRIPT, str(cdx.lib_path())],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
