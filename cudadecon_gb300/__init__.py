@@ -29,6 +29,8 @@ __all__ = [
     "rl_init",
     "rl_decon",
     "rl_cleanup",
+    "set_dft_form",
+    "dft_form",
     "output_shape",
     "deskew",
     "affine",
@@ -100,6 +102,10 @@ def _bind(L) -> None:
                                      POINTER(c_double), POINTER(c_longlong)]),
         "cdx_profile_pass_name": (c_char_p, [c_int]),
         "cdx_lambda_trace": (c_int, [c_int]),
+        "cdx_set_dft_form": (c_int, [c_int]),
+        "cdx_get_dft_form": (c_int, []),
+        "cdx_tc_length_supported": (c_int, [c_int]),
+        "cdx_tc_status": (c_int, []),
         "cdx_lambda_read": (c_int, [_F, c_int]),
         "cdx_deskew_device": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_void_p, c_int,
                                       c_int, c_float, c_void_p]),
@@ -242,6 +248,18 @@ def mip(volume, axis):
     if ok != 1:
         _err("cdx_mip_device")
     return out
+
+
+def set_dft_form(form: str) -> None:
+    """'plain' (FP32 CUDA-core FFT) or 'mixed' (tensor-core DFT stages in
+    split TF32 for the x rows that have a tensor-core plan)."""
+    code = {"plain": 0, "mixed": 1}[form]
+    if lib().cdx_set_dft_form(code) != 1:
+        _err("cdx_set_dft_form")
+
+
+def dft_form() -> str:
+    return "mixed" if lib().cdx_get_dft_form() == 1 else "plain"
 
 
 def rl_cleanup() -> None:

@@ -21,7 +21,7 @@ LIBNAME = "libcudaDecon.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE)]
-SOURCES = ["decon_kernels.cu", "decon_x_fwd.cu", "decon_x_ratio.cu", "decon_x_update.cu", "decon_y.cu", "decon_z.cu", "geometry.cu", "affine.cu", "accel.cu", "accel_noalloc.cu", "abi.cu", "otf_make.cu", "wiener.cu", "tiles.cu", "otf_io.cpp"]
+SOURCES = ["decon_kernels.cu", "decon_x_fwd.cu", "decon_x_ratio.cu", "decon_x_update.cu", "decon_x_tc.cu", "decon_y.cu", "decon_z.cu", "geometry.cu", "affine.cu", "accel.cu", "accel_noalloc.cu", "abi.cu", "otf_make.cu", "wiener.cu", "tiles.cu", "otf_io.cpp"]
 
 
 def nvcc() -> str:

@@ -745,12 +745,14 @@ struct Batch {
   cudaEvent_t ev_join[kBatchStreams] = {};
   cudaGraphExec_t exec = nullptr;
   int graph_iters = -1;
+  int graph_form = -1;  // DFT form the graph's kernels were captured with
   long long graph_launches = 0;
   long long last_launches = 0;
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
     graph_iters = -1;
+    graph_form = -1;
   }
   void release() {
     drop_graph();
@@ -896,6 +898,7 @@ static int batch_capture(Batch& b, int nIters) {
     return rc;
   }
   b.graph_iters = nIters;
+  b.graph_form = dft_form();
   b.graph_launches = launches;
   return 0;
 }
@@ -965,7 +968,7 @@ static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStrea
     launches += 2;
   }
   if (nIters > 0) {
-    if (!b.exec || b.graph_iters != nIters) {
+    if (!b.exec || b.graph_iters != nIters || b.graph_form != dft_form()) {
       // the plans' tables were built on the origin stream
       CDX_CHECK(cudaStreamSynchronize(b.origin));
       if ((rc = batch_capture(b, nIters))) return rc;
@@ -1031,6 +1034,7 @@ static int rl_common(const unsigned short* d_raw, const RLArgs& a, float* d_resu
       CDX_CHECK(cudaMemcpyAsync(h_deskewed, desk_dev, nd * sizeof(float), cudaMemcpyDeviceToHost,
                                 s.stream));
     CDX_CHECK(cudaStreamSynchronize(s.stream));
+    if (a.nIters > 0 && dft_form() == 1 && (rc = tc_check(s.plan.fx))) return rc;
   } else if (d_result && out != d_result) {
     CDX_CHECK(cudaMemcpyAsync(d_result, out, nout * sizeof(float), cudaMemcpyDeviceToDevice,
                               s.stream));
@@ -1115,6 +1119,31 @@ int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, dou
 }
 
 const char* cdx_profile_pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : ""; }
+
+int cdx_set_dft_form(int form) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (form != 0 && form != 1) {
+    set_error("cdx_set_dft_form", "form must be 0 (plain FP32) or 1 (mixed precision)");
+    return 0;
+  }
+  set_dft_form(form);
+  return 1;
+}
+
+int cdx_get_dft_form(void) { return dft_form(); }
+
+int cdx_tc_length_supported(int n) {
+  int q0 = 0, q1 = 0;
+  return tc_plan_radices(n, q0, q1) ? 1 : 0;
+}
+
+int cdx_tc_status(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!s.plan.valid) return 1;
+  if (s.stream) cudaStreamSynchronize(s.stream);
+  return tc_check(s.plan.fx) == 0 ? 1 : 0;
+}
 
 int cdx_lambda_trace(int n) {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -54,6 +54,44 @@ __device__ __forceinline__ void acc_add(float& hi, float& lo, float p) {
   lo = __fadd_rn(lo, err);
 }
 
+// Float-float accumulation of a second float-float value (hi, lo).
+__device__ __forceinline__ void ff_add(float4& s, float4 r) {
+  acc_add(s.x, s.y, r.x);
+  s.y = __fadd_rn(s.y, r.y);
+  acc_add(s.z, s.w, r.z);
+  s.w = __fadd_rn(s.w, r.w);
+}
+
+// Warp-wide float-float sum (tree over the lanes); result in lane 0.
+__device__ __forceinline__ float4 warp_sum2_ff(float4 s) {
+  for (int o = 16; o > 0; o >>= 1) {
+    float4 r;
+    r.x = __shfl_down_sync(0xffffffffu, s.x, o);
+    r.y = __shfl_down_sync(0xffffffffu, s.y, o);
+    r.z = __shfl_down_sync(0xffffffffu, s.z, o);
+    r.w = __shfl_down_sync(0xffffffffu, s.w, o);
+    ff_add(s, r);
+  }
+  return s;
+}
+
+// Block-wide sum of two float-float values (ah + al, bh + bl): a shuffle tree
+// in each warp, then one over the warps' sums, all with TwoSum in FP32
+// (GB300's FP64 rate is a small fraction of its FP32 rate).  Returns (sum a
+// hi, lo, sum b hi, lo), valid in thread 0.  The order of the additions is
+// fixed, so the result is the same on every run.
+__device__ __forceinline__ float4 block_sum2_ff(float ah, float al, float bh, float bl,
+                                               float4* red) {
+  float4 s = warp_sum2_ff(make_float4(ah, al, bh, bl));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = s;
+  __syncthreads();
+  if (warp == 0) s = warp_sum2_ff(lane < nw ? red[lane] : make_float4(0.f, 0.f, 0.f, 0.f));
+  return s;
+}
+
 // Prediction of the reference's updatePrediction_kernel (RLgpuImpl.cu:658-666):
 // Y = X + lambda*(X - X_{k-1}) with lambda as float, then clamped at 0.
 __device__ __forceinline__ float predict_y(float x, float xm1, float lam) {

@@ -106,8 +106,30 @@ int fft_len_init(FftLen& f, int L) {
   if (f.has_xr) {
     if (int rc = build_fft_dev(L, rad, f.xrdev, &f.d_twxr)) return rc;
   }
+  int q0 = 0, q1 = 0;
+  f.has_tc = tc_plan_radices(L, q0, q1);
+  if (f.has_tc) {
+    if (int rc = tc_tables_init(f.tc, L)) return rc;
+    CDX_CHECK(cudaMalloc(&f.tc.d_err, sizeof(int)));
+    CDX_CHECK(cudaMemset(f.tc.d_err, 0, sizeof(int)));
+  }
   return 0;
 }
+
+int tc_check(const FftLen& f) {
+  if (!f.has_tc || !f.tc.d_err) return 0;
+  int e = 0;
+  CDX_CHECK(cudaMemcpy(&e, f.tc.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    set_error("tensor-core x pass", "a wait on the tensor core ran out (result invalid)");
+    return cudaErrorLaunchTimeout;
+  }
+  return 0;
+}
+
+static int g_dft_form = 0;
+int dft_form() { return g_dft_form; }
+void set_dft_form(int form) { g_dft_form = form; }
 
 void fft_len_free(FftLen& f) {
   if (f.d_tw) cudaFree(f.d_tw);
@@ -121,6 +143,8 @@ void fft_len_free(FftLen& f) {
   f.xrdev.tw = nullptr;
   f.has_static = false;
   f.has_xr = false;
+  if (f.has_tc) tc_tables_free(f.tc);
+  f.has_tc = false;
 }
 
 // Row pairs per block of the x passes: the registered tile of a compile-time

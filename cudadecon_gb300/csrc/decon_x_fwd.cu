@@ -56,6 +56,8 @@ static int x_fwd_go(const Geom& g, const FftDev& f, const float* X, float* Xm1,
 
 int launch_x_fwd(const Geom& g, const FftLen& fx, const float* X, float* Xm1,
                  const float* lam, int predict, float2* S, cudaStream_t st) {
+  if (fx.has_tc && dft_form() == 1)
+    return launch_xtc_fwd(g, fx.tc, X, Xm1, lam, predict, S, fx.tc.d_err, st);
   if (fx.has_static) switch (g.nx) {
 #define CDX_CASE(L, PP)                                                                      \
   case L:                                                                                    \

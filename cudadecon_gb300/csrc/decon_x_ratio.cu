@@ -49,6 +49,8 @@ static int x_ratio_go(const Geom& g, const FftDev& f, float2* S, const float* ra
 
 int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const float* raw,
                            float eps, cudaStream_t st) {
+  if (fx.has_tc && dft_form() == 1)
+    return launch_xtc_ratio(g, fx.tc, S, raw, eps, fx.tc.d_err, st);
   if (fx.has_xr) switch (g.nx) {
 #define CDX_XR_CASE(L, PP, ...)                                                            \
   case L:                                                                                  \

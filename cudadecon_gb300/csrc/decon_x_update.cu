@@ -5,44 +5,6 @@
 
 namespace cdx {
 
-// Float-float accumulation of a second float-float value (hi, lo).
-__device__ __forceinline__ void ff_add(float4& s, float4 r) {
-  acc_add(s.x, s.y, r.x);
-  s.y = __fadd_rn(s.y, r.y);
-  acc_add(s.z, s.w, r.z);
-  s.w = __fadd_rn(s.w, r.w);
-}
-
-// Warp-wide float-float sum (tree over the lanes); result in lane 0.
-__device__ __forceinline__ float4 warp_sum2_ff(float4 s) {
-  for (int o = 16; o > 0; o >>= 1) {
-    float4 r;
-    r.x = __shfl_down_sync(0xffffffffu, s.x, o);
-    r.y = __shfl_down_sync(0xffffffffu, s.y, o);
-    r.z = __shfl_down_sync(0xffffffffu, s.z, o);
-    r.w = __shfl_down_sync(0xffffffffu, s.w, o);
-    ff_add(s, r);
-  }
-  return s;
-}
-
-// Block-wide sum of two float-float values (ah + al, bh + bl): a shuffle tree
-// in each warp, then one over the warps' sums, all with TwoSum in FP32
-// (GB300's FP64 rate is a small fraction of its FP32 rate).  Returns (sum a
-// hi, lo, sum b hi, lo), valid in thread 0.  The order of the additions is
-// fixed, so the result is the same on every run.
-__device__ __forceinline__ float4 block_sum2_ff(float ah, float al, float bh, float bl,
-                                               float4* red) {
-  float4 s = warp_sum2_ff(make_float4(ah, al, bh, bl));
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nw = (blockDim.x + 31) >> 5;
-  __syncthreads();
-  if (lane == 0) red[warp] = s;
-  __syncthreads();
-  if (warp == 0) s = warp_sum2_ff(lane < nw ? red[lane] : make_float4(0.f, 0.f, 0.f, 0.f));
-  return s;
-}
-
 // The next acceleration factor from the blocks' partial sums (one float4 per
 // update block): sums in a fixed order, then calcAccelFactor
 // (RLgpuImpl.cu:565) in double and the clamp of RL-Biggs-Andrews.cpp:298.
@@ -183,17 +145,21 @@ static int x_update_go(const Geom& g, const FftDev& f, const float2* S, const fl
   CDX_CHECK(launch_pdl(k_x_inv_update<Run>, grid, dim3(T), smem, st, g, f, S, Y, Xout, G, dots,
                        part, P));
   CDX_LAUNCH_CHECK("k_x_inv_update");
-  if (dots) {
-    CDX_CHECK(launch_pdl(k_lambda, dim3(1), dim3(1024), 0, st, (const float4*)part, nblk, lam_next,
-                         eps));
-    CDX_LAUNCH_CHECK("k_lambda");
-  }
+  if (dots) return launch_lambda(part, nblk, lam_next, eps, st);
+  return 0;
+}
+
+int launch_lambda(const float4* partials, int nblk, float* lam_next, float eps, cudaStream_t st) {
+  CDX_CHECK(launch_pdl(k_lambda, dim3(1), dim3(1024), 0, st, partials, nblk, lam_next, eps));
+  CDX_LAUNCH_CHECK("k_lambda");
   return 0;
 }
 
 int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* Y,
                         float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
                         cudaStream_t st) {
+  if (fx.has_tc && dft_form() == 1)
+    return launch_xtc_update(g, fx.tc, S, Y, Xout, G, dots, w, lam_next, eps, fx.tc.d_err, st);
   if (fx.has_xr) switch (g.nx) {
 #define CDX_XR_CASE(L, PP, ...)                                                                 \
   case L:                                                                                       \

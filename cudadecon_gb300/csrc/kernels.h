@@ -40,6 +40,25 @@ struct RawOtfDims {
   float kxscale, kyscale, kzscale;
 };
 
+// Tables of a tensor-core row plan (mixed-precision form, decon_x_tc.cu):
+// the DFT matrices of the two radices as tf32 hi/lo MMA operands, the
+// twiddles, and an error word the kernels set when a wait on the tensor
+// core runs out.
+struct TcTables {
+  int q0 = 0, q1 = 0;
+  float* d_b = nullptr;
+  float2* d_tw = nullptr;
+  int* d_err = nullptr;
+};
+bool tc_plan_radices(int L, int& q0, int& q1);
+int tc_tables_init(TcTables& t, int L);
+void tc_tables_free(TcTables& t);
+
+// Which form the x passes take: 0 = plain FP32 (CUDA-core FFT), 1 = mixed
+// precision (tensor-core DFT stages where the length has a tensor-core plan).
+int dft_form();
+void set_dft_form(int form);
+
 // FFT plan for one length (host side owns the twiddle table).
 // When the length is in the registry of specialised plans (static_plans.cuh),
 // sdev holds that plan (its radices and twiddle table) as well.
@@ -53,6 +72,9 @@ struct FftLen {
   bool has_xr = false;
   FftDev xrdev;
   float2* d_twxr = nullptr;
+  // the tensor-core plan of the length, if it has one
+  bool has_tc = false;
+  TcTables tc;
 };
 int fft_len_init(FftLen& f, int L);
 void fft_len_free(FftLen& f);
@@ -91,6 +113,21 @@ int launch_x_inv_ratio_fwd(const Geom& g, const FftLen& fx, float2* S, const flo
 int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const float* Y,
                         float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
                         cudaStream_t st);
+// The next acceleration factor from nblk float-float partials (one block).
+int launch_lambda(const float4* partials, int nblk, float* lam_next, float eps, cudaStream_t st);
+// The x passes in the mixed-precision form (same contracts as the three
+// launchers above; err: the plan's error word).
+int launch_xtc_fwd(const Geom& g, const TcTables& t, const float* X, float* Xm1, const float* lam,
+                   int predict, float2* S, int* err, cudaStream_t st);
+int launch_xtc_ratio(const Geom& g, const TcTables& t, float2* S, const float* raw, float eps,
+                     int* err, cudaStream_t st);
+int launch_xtc_update(const Geom& g, const TcTables& t, const float2* S, const float* Y,
+                      float* Xout, float* G, int dots, RLWork& w, float* lam_next, float eps,
+                      int* err, cudaStream_t st);
+// 0 when no tensor-core wait of the plan has run out (reads the error word;
+// synchronises the device).
+int tc_check(const FftLen& f);
+
 // Plain inverse x pass to a real volume (test path).
 int launch_x_inv_plain(const Geom& g, const FftLen& fx, const float2* S, float* out,
                        cudaStream_t st);

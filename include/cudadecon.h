@@ -133,6 +133,24 @@ int cdx_profile_read(double* pass_ms, long long* pass_count, int max_passes, dou
                      long long* iter_count);
 const char* cdx_profile_pass_name(int i);
 
+/* Form of the DFTs of the x passes (extension; the reference runs cuFFT in
+ * FP32): 0 = plain FP32 on the CUDA cores (default); 1 = mixed
+ * precision, where rows whose length has a tensor-core plan
+ * (cdx_tc_length_supported: 256, 512, 756, 1024) run their DFT stages as
+ * tcgen05 MMAs in TF32 with each FP32 operand split into a high and a low
+ * part (three products, FP32 accumulation; relative error of the transforms
+ * about 1e-6).  Other passes and lengths stay on the CUDA cores.  The form
+ * applies to every later RL call of the process.  cdx_set_dft_form returns 0
+ * for another value. */
+int cdx_set_dft_form(int form);
+int cdx_get_dft_form(void);
+int cdx_tc_length_supported(int n);
+/* 1 when no wait on the tensor core of the current session has run out
+ * (the kernels bound every wait to about a second and then give up; the
+ * result of such a call is invalid).  Waits for the session's stream.
+ * RL_interface checks this itself and returns 0. */
+int cdx_tc_status(void);
+
 /* Trace of the Biggs-Andrews acceleration factors (extension; the reference
  * prints them, RL-Biggs-Andrews.cpp:300).  cdx_lambda_trace(n) with n > 0
  * makes every later RL call record, for iteration k < n, the factor lambda_k
