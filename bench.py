@@ -1,28 +1,39 @@
 #!/usr/bin/env python3
-"""Benchmark: Richardson-Lucy voxel-iterations/s on the stage-scan light-sheet
-workload (101x256x512 uint16 raw at 31.5 deg, dz 0.3 um, dxy 0.104 um ->
-deskew to 100x256x756, 15 Biggs-Andrews RL iterations, rotate to
-150x256x723), synthetic seeded data.
+"""Benchmark: Richardson-Lucy voxel-iterations/s, batched uneven stacks in
+the plain FP32 and the mixed-precision forms.
 
-One step = one full pass of the hot path over the stack: crop, background
-subtraction, deskew, 15 RL iterations, rotation.
+Headline workload (one step = one call that deconvolves every stack):
+64 synthetic stacks of uneven shape, z from the 2,3,5,7-smooth sizes in
+[32, 160], y in [128, 512], x in [128, 1024] (seeded), each with its own
+Gaussian OTF (sigmas jittered by +-20%), uint16 with a Poisson background
+and sparse beads, 10 Biggs-Andrews RL iterations, through
+cdx_RL_batch_device (one CUDA graph of every stack's iterations).
 
-  value : inputs already resident in HBM, cdx_RL_device on a stream, timed
-          with CUDA events (device time), voxel-iterations/s of the decon grid
-  e2e   : RL_interface (the reference's C entry point) with pinned host
-          buffers, host<->device copies inside the timed region; also with
-          pageable numpy buffers (e2e.pageable)
-  roofline : one RL iteration against the measured HBM copy bandwidth, with
-          56 B of algorithmic traffic per voxel-iteration, timed per pass with
-          CUDA events recorded by the library on its launch stream
-  cpu_baseline : the CPU restatement (scipy.fft float32, all host cores) on
-          a bounded sample (at least 10 s of iterations) of the same volume
+  value   : plain FP32 form, stacks resident in HBM, CUDA events on the
+            launch stream; voxel-iterations/s of all decon grids
+  forms   : the same in the mixed-precision form (x-pass DFT stages as
+            tcgen05 MMAs in split TF32) and the ratio mixed / plain
+  e2e     : the same call with host buffers: each step copies the 64 raw
+            stacks in from pinned host memory and the 64 results out
+  roofline: 56 B of algorithmic traffic per voxel-iteration over the
+            measured HBM copy bandwidth, for the batch step; the per-pass
+            roofline of one iteration is in secondary.stage_scan
+  secondary:
+    stage_scan : 101x256x512 u16 at 31.5 deg -> deskew to 100x256x756,
+                 15 iterations, rotate (single stack, RL_interface and
+                 cdx_RL_device; pinned and pageable e2e; per-pass timing)
+    grid_128x512x1024 : 20 iterations, plain and mixed forms
+    timelapse  : 8 timepoints x 2 channels of 256x1024x1024 u16: camcor,
+                 deskew (-> 256x1024x1620), 20 iterations, rotate, with
+                 one OTF per channel
+  cpu_baseline : the CPU restatement in oracle/ (scipy.fft float32, all
+                 host cores) on a bounded sample of the stage-scan volume
 
---impl reference times the reference's own implementation of the path: its
-CUDA kernels (compiled to PTX from its sources) with cuFFT, launched in the
-order of RichardsonLucy_GPU's host code on the same workload (the reference
-has no CPU implementation of this loop).  cpu_baseline, in both arms, is the
-CPU restatement in oracle/ (scipy.fft float32, all host cores).
+--impl reference times the reference's own implementation of the path on
+the same batch: its CUDA kernels (compiled to PTX from its sources) with
+cuFFT, launched in the order of one RL_interface call per stack
+(oracle/ref_runner.cu), one reference session (plans, OTF, buffers) per
+stack; the reference has no CPU implementation of this loop.
 
 Multi-GPU: independent stacks do not exchange data, so N ranks run N
 replicas (weak scaling); value is the work of all ranks over the slowest
@@ -35,7 +46,6 @@ import argparse
 import ctypes
 import datetime
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -50,13 +60,22 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 ALG_BYTES_PER_VOXEL_ITER = 56.0  # one fused iteration, float32 storage
+NOMINAL_HBM_GBS = 8000.0         # GB300's nominal HBM3e bandwidth
 
-WORKLOAD = dict(
+BATCH = {"stacks": 64, "iterations": 10, "seed": 1003, "z": (32, 160), "y": (128, 512),
+         "x": (128, 1024)}
+BATCH_NAME = (f"{BATCH['stacks']} uneven stacks, z/y/x 2-3-5-7-smooth in {BATCH['z']}/"
+              f"{BATCH['y']}/{BATCH['x']}, own Gaussian OTF each, {BATCH['iterations']} RL it")
+
+STAGE = dict(
     name="stage-scan light-sheet 101x256x512 u16, deskew 31.5deg -> 100x256x756, 15 RL it, rotate",
     raw_shape=(101, 256, 512), dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.2, angle=31.5,
     background=100.0, n_iters=15, otf_nr=129, otf_nz=64, psf_sigma_xy=1.3, psf_sigma_z=3.0,
     seed=1002,
 )
+GRID3 = dict(shape=(128, 512, 1024), n_iters=20, seed=1003)
+LAPSE = dict(timepoints=8, channels=2, shape=(256, 1024, 1024), n_iters=20, angle=31.5,
+             dr=0.104, dz=0.3, seed=1005)
 
 
 def peaks():
@@ -67,9 +86,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def make_inputs(tmpdir):
+# ---------------------------------------------------------------- inputs
+def stage_inputs(tmpdir):
     from cudadecon_gb300 import synth
-    w = WORKLOAD
+    w = STAGE
     raw = synth.bead_stack(w["raw_shape"], n_beads=300, sigma_range=(0.5, 2.0),
                            amp_range=(500.0, 5000.0), psf_sigma_xy=w["psf_sigma_xy"],
                            psf_sigma_z=w["psf_sigma_z"], background=w["background"],
@@ -78,6 +98,25 @@ def make_inputs(tmpdir):
     otf_path = Path(tmpdir) / "otf.tif"
     synth.write_otf(otf_path, tab)
     return raw, tab, otf_path
+
+
+def batch_inputs(dev):
+    """The 64 stacks (device u16 tensors) with their OTF tables, seeded."""
+    import torch
+    from cudadecon_gb300 import synth
+    rng = np.random.default_rng(BATCH["seed"])
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(BATCH["seed"])
+    stacks = []
+    for _ in range(BATCH["stacks"]):
+        shape = tuple(int(rng.choice(synth.smooth_sizes(*BATCH[a]))) for a in ("z", "y", "x"))
+        j = rng.uniform(0.8, 1.2, 2)
+        tab = synth.gaussian_otf_table(129, 64, 1.5 * j[0], 4.0 * j[1])
+        lam = 100.0 + 3000.0 * (torch.rand(shape, generator=gen, device=dev) < 2e-4).float()
+        raw = torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.uint16)
+        stacks.append(dict(raw=raw, otf=tab, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.3,
+                           background=100.0))
+    return stacks
 
 
 class ClockSampler:
@@ -149,11 +188,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ---------------------------------------------------------------- CPU baseline
 def cpu_prepare(raw, tab):
     """CPU-baseline leg: the oracle's deskewed start volume and OTF grid."""
     from oracle import rl_oracle as O
     from cudadecon_gb300 import synth
-    w = WORKLOAD
+    w = STAGE
     nz, ny, nx = w["raw_shape"]
     st = O.rl_init(nx, ny, nz, w["dr"], w["dz"], w["dr_psf"], w["dz_psf"], w["angle"], w["angle"],
                    0, False, synth.otf_table_to_image(tab))
@@ -184,6 +224,21 @@ def cpu_time_bounded(X, H, workers, min_s=10.0, chunk=5, max_iters=60):
     return X.size * n / t, t, n
 
 
+def cpu_baseline_leg(min_s=10.0):
+    """The oracle's float32 iteration (scipy.fft, all host cores) on a bounded
+    sample of the stage-scan deskewed volume."""
+    with tempfile.TemporaryDirectory() as td:
+        raw, tab, _ = stage_inputs(td)
+    cores = os.cpu_count() or 1
+    X, H = cpu_prepare(raw, tab)
+    cpu_time_iterations(X, H, 1, cores)  # warm-up (FFT plans, page faults)
+    v, dt, n = cpu_time_bounded(X, H, cores, min_s=min_s)
+    return {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
+            "sample": f"{n} RL iterations (runs of 5) on the stage-scan deskewed {X.size}-voxel "
+                      f"volume (scipy.fft float32, {cores} threads), {dt:.1f} s"}
+
+
+# ---------------------------------------------------------------- distribution
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -209,18 +264,19 @@ def max_over_ranks(x, pg, device="cpu"):
     return float(t.item())
 
 
-def cpu_baseline_leg(raw, tab, min_s=10.0):
-    """The oracle's float32 iteration (scipy.fft, all host cores) on a bounded
-    sample of the workload's deskewed volume."""
-    cores = os.cpu_count() or 1
-    X, H = cpu_prepare(raw, tab)
-    cpu_time_iterations(X, H, 1, cores)  # warm-up (FFT plans, page faults)
-    v, dt, n = cpu_time_bounded(X, H, cores, min_s=min_s)
-    return {"value": v, "unit": "voxel-iter/s", "cores": cores, "kind": "port",
-            "sample": f"{n} RL iterations (runs of 5 of the {WORKLOAD['n_iters']}) on the deskewed "
-                      f"{X.size}-voxel volume (scipy.fft float32, {cores} threads), {dt:.1f} s"}
+def events_ms(torch, stream, fn, reps):
+    """Average milliseconds of fn() over reps calls, CUDA events on stream."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
 
 
+# ---------------------------------------------------------------- reference arm
 def reference_gpu_available():
     try:
         import torch
@@ -233,37 +289,30 @@ def reference_gpu_available():
 
 
 def run_reference(args):
-    """The reference's own implementation of the path.  Its RL loop exists only
-    on the GPU (its kernels with cuFFT, src/RL-Biggs-Andrews.cpp:56-450); the
-    reference's CUDA sources are compiled to PTX and launched in the order of
-    its host code by oracle/ref_runner.cu (a replay of one RL_interface call:
-    background subtraction, bleach statistic, deskew, the loop with the
-    per-iteration host round trip for lambda, rotation), on buffers and cuFFT
-    plans made once.  value: device-resident raw stack, CUDA events; e2e: the
-    float stack copied in and the result copied out (pinned buffers) inside
-    the timed region.  Where the reference runner is not built, the timed arm
-    is the CPU restatement (oracle port)."""
+    """The reference's own implementation of the path.  Its RL loop exists
+    only on the GPU (its kernels with cuFFT, src/RL-Biggs-Andrews.cpp:56-450):
+    the reference's CUDA sources compiled to PTX and launched in the order of
+    its host code by oracle/ref_runner.cu, one session (buffers, cuFFT plans,
+    OTF array, as RL_interface_init) per stack, one RL_interface call's device
+    work per stack and step.  Where the reference runner is not built, the
+    timed arm is the CPU restatement (oracle port) on the stage-scan volume."""
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
         if pg:
             pg.barrier()
         return 0
-    with tempfile.TemporaryDirectory() as td:
-        raw, tab, _ = make_inputs(td)
-    cpu = None if args.no_cpu_baseline else cpu_baseline_leg(raw, tab)
+    cpu = None if args.no_cpu_baseline else cpu_baseline_leg()
     ok, why = reference_gpu_available()
-    w = WORKLOAD
-    nz, ny, nx = w["raw_shape"]
     common = {"impl": "reference", "metric": "RL voxel-iterations/s", "unit": "voxel-iter/s",
               "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-              "data": "synthetic (seeded beads + filaments)"}
+              "data": "synthetic (seeded)"}
     if not ok:
         if cpu is None:
-            cpu = cpu_baseline_leg(raw, tab)
+            cpu = cpu_baseline_leg()
         v = cpu["value"]
         line = dict(common, value=v, ms_per_step=None,
-                    config={"workload": WORKLOAD["name"], "l2_policy": "n/a (CPU)",
+                    config={"workload": STAGE["name"], "l2_policy": "n/a (CPU)",
                             "reference_gpu_unavailable": why},
                     cpu_baseline=cpu,
                     e2e={"value": v, "unit": "voxel-iter/s", "h2d_bytes_per_step": 0,
@@ -277,169 +326,125 @@ def run_reference(args):
     from oracle import ref_kernels as RK
     from oracle import rl_oracle as O
     torch.cuda.set_device(local)
-    st = O.rl_init(nx, ny, nz, w["dr"], w["dz"], w["dr_psf"], w["dz_psf"], w["angle"], w["angle"],
-                   0, False, synth.otf_table_to_image(tab))
-    sess = RK.Session(st)
-    rawf = np.ascontiguousarray(raw[:st.output_nz, :st.output_ny, :st.output_nx], np.float32)
-    d_raw = torch.from_numpy(rawf).cuda()
-    d_out = torch.empty(sess.out_shape, dtype=torch.float32, device="cuda")
-    n_iters = w["n_iters"]
-    bg = w["background"]
+    dev = torch.device("cuda", local)
+    stacks = batch_inputs(dev)
+    n_iters = BATCH["iterations"]
+    sess, raws, outs, vox = [], [], [], 0
+    for d in stacks:
+        nz, ny, nx = d["raw"].shape
+        st = O.rl_init(nx, ny, nz, d["dr"], d["dz"], d["dr_psf"], d["dz_psf"], 0.0, 0.0, 0, False,
+                       synth.otf_table_to_image(d["otf"]))
+        s = RK.Session(st)
+        gz, gy, gx = s.raw_shape
+        raws.append(d["raw"][:gz, :gy, :gx].float().contiguous())
+        outs.append(torch.empty(s.out_shape, dtype=torch.float32, device=dev))
+        sess.append(s)
+        vox += int(np.prod(s.grid))
+    del stacks
+
+    def step():
+        for s, r, o in zip(sess, raws, outs):
+            s.step(r, 100.0, n_iters, o)
+
     for _ in range(args.warmup):
-        sess.step(d_raw, bg, n_iters, d_out)
+        step()
     torch.cuda.synchronize()
     clk = ClockSampler(local)
     clk.start()
     time.sleep(0.3)  # nvidia-smi's first row
     t_wall0 = time.time()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        sess.step(d_raw, bg, n_iters, d_out)
-    e1.record()
-    e1.synchronize()
+    ms = events_ms(torch, torch.cuda.current_stream(), step, args.steps)
     t_wall1 = time.time()
     clocks = clk.stop(t_wall0, t_wall1)
-    ms = e0.elapsed_time(e1) / args.steps
-    gz, gy, gx = sess.grid
-    vox_iters = gz * gy * gx * n_iters
-    value = vox_iters / (ms * 1e-3)
-    finite = bool(torch.isfinite(d_out).all().item())
-    # per iteration: the same call without iterations, subtracted
-    sess.step(d_raw, bg, 0, d_out)
-    e0.record()
-    for _ in range(args.steps):
-        sess.step(d_raw, bg, 0, d_out)
-    e1.record()
-    e1.synchronize()
-    prepost_ms = e0.elapsed_time(e1) / args.steps
-    iter_ms = (ms - prepost_ms) / n_iters
-    # e2e: float stack in, result out, through pinned host buffers
-    h_raw = torch.from_numpy(rawf).pin_memory()
-    h_out = torch.empty(sess.out_shape, dtype=torch.float32).pin_memory()
+    value = vox * n_iters / (ms * 1e-3)
+    finite = all(bool(torch.isfinite(o).all().item()) for o in outs)
+    # e2e: the float stacks in and the results out through pinned host buffers
+    h_in = [r.cpu().pin_memory() for r in raws]
+    h_out = [torch.empty(o.shape, dtype=torch.float32).pin_memory() for o in outs]
     torch.cuda.synchronize()
+    reps = max(1, min(args.steps, 5))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        d_raw.copy_(h_raw)
-        sess.step(d_raw, bg, n_iters, d_out)
-        h_out.copy_(d_out)
+    for _ in range(reps):
+        for s, hi, r, o, ho in zip(sess, h_in, raws, outs, h_out):
+            r.copy_(hi)
+            s.step(r, 100.0, n_iters, o)
+            ho.copy_(o)
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    sess.close()
+    e2e_s = (time.perf_counter() - t0) / reps
+    for s in sess:
+        s.close()
     line = dict(common, value=value, ms_per_step=ms,
-                config={"workload": WORKLOAD["name"], "decon_grid_zyx": [gz, gy, gx],
+                config={"workload": BATCH_NAME, "stacks": BATCH["stacks"], "decon_voxels": vox,
                         "iterations": n_iters, "form": "reference kernels + cuFFT (plain FP32)",
                         "reference_impl": "src/RLgpuImpl.cu, geometryTransform.cu compiled to PTX "
                                           "from the reference's sources, launched in the order of "
-                                          "RichardsonLucy_GPU (oracle/ref_runner.cu); buffers and "
-                                          "cuFFT plans made once",
-                        "l2_policy": "working set ~0.5 GB > 129 MB L2 (no flush needed)"},
-                iteration_ms=iter_ms, prepost_ms_per_step=prepost_ms,
+                                          "RichardsonLucy_GPU (oracle/ref_runner.cu); one session "
+                                          "(buffers, cuFFT plans, OTF) per stack, made once",
+                        "l2_policy": "working set ~30 GB > 129 MB L2 (no flush needed)"},
                 cpu_baseline=cpu, clocks=clocks, output_finite=finite,
-                e2e={"value": vox_iters / e2e_s, "unit": "voxel-iter/s",
-                     "h2d_bytes_per_step": int(rawf.nbytes),
-                     "d2h_bytes_per_step": int(h_out.numel() * 4)})
+                e2e={"value": vox * n_iters / e2e_s, "unit": "voxel-iter/s",
+                     "h2d_bytes_per_step": int(sum(r.numel() * 4 for r in raws)),
+                     "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in outs))})
     print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
     return 0
 
 
-# GB300's nominal HBM3e bandwidth, for the fraction against the nominal figure
-# (the roofline's peak is the measured copy bandwidth)
-NOMINAL_HBM_GBS = 8000.0
-
-BATCH = {"stacks": 64, "iterations": 10, "seed": 1003, "z": (32, 160), "y": (128, 512),
-         "x": (128, 1024)}
-
-
-def run_batch(cdx, dev, reps=3):
-    """64 uneven stacks with their own OTFs through cdx_RL_batch_device
-    (one CUDA graph per call), and the same stacks through per-stack calls
-    (RL_interface_init + cdx_RL_device each) for comparison.  Stacks are a
-    Poisson background plus sparse point beads, generated on the GPU (seeded);
-    OTFs are Gaussian with sigmas jittered by +-20%."""
-    import torch
-    from cudadecon_gb300 import synth
-    rng = np.random.default_rng(BATCH["seed"])
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(BATCH["seed"])
-    stacks, vox = [], 0
-    for _ in range(BATCH["stacks"]):
-        shape = tuple(int(rng.choice(synth.smooth_sizes(*BATCH[a]))) for a in ("z", "y", "x"))
-        j = rng.uniform(0.8, 1.2, 2)
-        tab = synth.gaussian_otf_table(129, 64, 1.5 * j[0], 4.0 * j[1])
-        lam = 100.0 + 3000.0 * (torch.rand(shape, generator=gen, device=dev) < 2e-4).float()
-        raw = torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.uint16)
-        stacks.append(dict(raw=raw, otf=tab, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.3,
-                           background=100.0))
-        vox += int(np.prod(cdx.batch_grid(shape)))
+# ---------------------------------------------------------------- our arm
+def measure_batch(cdx, torch, dev, stream, stacks, steps, warmup, form):
+    """cdx_RL_batch_device over all stacks, device-resident: (ms per call,
+    voxel-iterations per call, launches per call, outputs finite)."""
+    L = cdx.lib()
+    assert L.cdx_set_dft_form(form) == 1
     iters = BATCH["iterations"]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    outs = cdx.rl_batch(stacks, n_iters=iters)
-    torch.cuda.synchronize()
-    first_s = time.perf_counter() - t0
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    st = torch.cuda.current_stream()
-    e0.record(st)
-    for _ in range(reps):
-        outs = cdx.rl_batch(stacks, n_iters=iters)
-    e1.record(st)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+    vox = sum(int(np.prod(cdx.batch_grid(tuple(d["raw"].shape)))) for d in stacks)
+    outs = cdx.rl_batch(stacks, n_iters=iters, stream=stream)
+    for _ in range(warmup):
+        outs = cdx.rl_batch(stacks, n_iters=iters, stream=stream)
+    stream.synchronize()
+    ms = events_ms(torch, stream, lambda: cdx.rl_batch(stacks, n_iters=iters, stream=stream),
+                   steps)
+    launches = int(L.cdx_batch_last_launch_count())
     finite = all(bool(torch.isfinite(o).all().item()) for o in outs)
-    launches = int(cdx.lib().cdx_batch_last_launch_count())
-    del outs
-    cdx.lib().cdx_batch_release()
-    # the same stacks one call at a time, as a per-stack caller does
-    L = cdx.lib()
-    with tempfile.TemporaryDirectory() as td:
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for i, d in enumerate(stacks):
-            p = Path(td) / f"otf{i}.tif"
-            synth.write_otf(p, d["otf"])
-            nz, ny, nx = d["raw"].shape
-            cdx.rl_init((nz, ny, nx), p, dr=d["dr"], dz=d["dz"], dr_psf=d["dr_psf"],
-                        dz_psf=d["dz_psf"], deskew_angle=0.0, rotation_angle=0.0)
-            out = torch.empty(cdx.output_shape(), dtype=torch.float32, device=dev)
-            ok = L.cdx_RL_device(ctypes.c_void_p(d["raw"].data_ptr()), nx, ny, nz,
-                                 ctypes.c_void_p(out.data_ptr()), None, d["background"], False,
-                                 False, iters, 0, 0, 0, 0.0, False, False,
-                                 ctypes.c_void_p(st.cuda_stream))
-            if ok != 1:
-                raise RuntimeError(L.cdx_last_error().decode())
-        torch.cuda.synchronize()
-        seq_s = time.perf_counter() - t0
-    cdx.rl_cleanup()
-    return {"workload": f"{BATCH['stacks']} uneven stacks, z/y/x 2-3-5-7-smooth in "
-                        f"{BATCH['z']}/{BATCH['y']}/{BATCH['x']}, own Gaussian OTF each, "
-                        f"{iters} RL iterations",
-            "decon_voxels": vox, "value": vox * iters / (ms * 1e-3), "unit": "voxel-iter/s",
-            "ms_per_call": ms, "first_call_s": first_s, "graph_launches_per_call": launches,
-            "per_stack_calls_value": vox * iters / seq_s, "per_stack_calls_s": seq_s,
-            "data": "synthetic: Poisson background 100 plus sparse point beads, seeded, on the GPU",
-            "output_finite": finite}
+    L.cdx_set_dft_form(0)
+    return ms, vox * iters, launches, finite
 
 
-def run_gb300(args):
-    import torch
-    world, rank, local, pg = dist_setup(args)
-    torch.cuda.set_device(local)
-    import cudadecon_gb300 as cdx
+def measure_batch_e2e(cdx, torch, dev, stream, stacks, reps):
+    """The batch with host buffers: pinned u16 stacks copied in, results out,
+    inside the timed region (wall clock)."""
+    iters = BATCH["iterations"]
+    h_raw = [d["raw"].cpu().pin_memory() for d in stacks]
+    dev_stacks = [dict(d) for d in stacks]
+    outs = cdx.rl_batch(dev_stacks, n_iters=iters, stream=stream)
+    h_out = [torch.empty(o.shape, dtype=torch.float32).pin_memory() for o in outs]
+    stream.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            for d, h in zip(dev_stacks, h_raw):
+                d["raw"].copy_(h, non_blocking=True)
+            outs = cdx.rl_batch(dev_stacks, n_iters=iters, stream=stream)
+            for o, h in zip(outs, h_out):
+                h.copy_(o, non_blocking=True)
+        stream.synchronize()
+    s = (time.perf_counter() - t0) / reps
+    return s, int(sum(h.numel() * 2 for h in h_raw)), int(sum(h.numel() * 4 for h in h_out))
+
+
+def measure_stage_scan(cdx, torch, dev, steps, pg):
+    """The single stage-scan stack: device-resident step, one iteration's time
+    and per-pass timing, e2e through RL_interface (pinned and pageable)."""
     L = cdx.lib()
-    w = WORKLOAD
+    w = STAGE
     nz, ny, nx = w["raw_shape"]
     td = tempfile.TemporaryDirectory()
-    raw, tab, otf_path = make_inputs(td.name)
+    raw, tab, otf_path = stage_inputs(td.name)
     cdx.rl_init(w["raw_shape"], otf_path, dr=w["dr"], dz=w["dz"], dr_psf=w["dr_psf"],
                 dz_psf=w["dz_psf"], deskew_angle=w["angle"], rotation_angle=w["angle"])
     onz, ony, onx = cdx.output_shape()
     gz, gy, gx = cdx.decon_grid()
-    dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     d_raw = torch.from_numpy(raw).to(dev)
@@ -453,51 +458,16 @@ def run_gb300(args):
         if ok != 1:
             raise RuntimeError(L.cdx_last_error().decode())
 
-    torch.cuda.synchronize()
-    clk = ClockSampler(local)
-    clk.start()
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(3):
             step()
     stream.synchronize()
-    launches_per_step = int(L.cdx_last_launch_count())
-    grid_vox = gz * gy * gx
-    # ---- timed region (device-resident inputs)
-    if pg:
-        pg.barrier()
-    torch.cuda.synchronize()
-    t_wall0 = time.time()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    e1.synchronize()
-    torch.cuda.synchronize()
-    t_wall1 = time.time()
-    dev_ms = e0.elapsed_time(e1)
-    clocks = clk.stop(t_wall0, t_wall1)
-    dev_ms = max_over_ranks(dev_ms, pg, dev)
-    ms_per_step = dev_ms / args.steps
-    vox_iters = grid_vox * n_iters
-    value = world * vox_iters / (ms_per_step / 1000.0)
-    finite = bool(torch.isfinite(d_out).all().item())
-
-    # ---- one RL iteration: the same call without iterations (crop, background,
-    # deskew, rotate only) timed the same way; the difference over n_iters is
-    # the iteration time with the passes chained as in the timed run
-    with torch.cuda.stream(stream):
-        step(0)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step(0)
-    e1.record(stream)
-    e1.synchronize()
-    prepost_ms = e0.elapsed_time(e1) / args.steps
-    iter_ms = (ms_per_step - prepost_ms) / n_iters
-
-    # ---- per-pass timing of the iteration (CUDA events on the library's launch stream)
+    ms = events_ms(torch, stream, step, steps)
+    prepost = events_ms(torch, stream, lambda: step(0), steps)
+    iter_ms = (ms - prepost) / n_iters
+    vox = gx * gy * gz
+    # per-pass timing (events between the passes break the programmatic
+    # launch chain, so the profiled iteration is a little slower)
     L.cdx_profile_enable(1)
     with torch.cuda.stream(stream):
         for _ in range(2):
@@ -509,124 +479,267 @@ def run_gb300(args):
     it_n = ctypes.c_longlong(0)
     L.cdx_profile_read(pm, pn, 9, ctypes.byref(it_ms), ctypes.byref(it_n))
     L.cdx_profile_enable(0)
-    # events between the passes break the programmatic launch chain, so the
-    # profiled iteration is a little slower than the chained one
-    iter_ms_profiled = it_ms.value / max(it_n.value, 1)
-    # bytes per voxel moved by each pass as built: x forward reads X, X_{k-1} and
-    # writes the spectrum and the prediction Y; x update reads the spectrum, Y
-    # and G_{k-1} and writes X_{k+1} and G_k
     pass_bytes = [16, 8, 8, 8, 12, 8, 8, 8, 20]
     passes = {}
     for i in range(9):
-        ms = pm[i] / max(pn[i], 1)
+        pms = pm[i] / max(pn[i], 1)
         passes[L.cdx_profile_pass_name(i).decode()] = {
-            "ms": round(ms, 5), "bytes_per_voxel": pass_bytes[i],
-            "gbs": round(pass_bytes[i] * grid_vox / (ms * 1e-3) / 1e9, 1) if ms > 0 else None}
-    hbm, peak_kind = peaks()
-    achieved = ALG_BYTES_PER_VOXEL_ITER * grid_vox / (iter_ms * 1e-3) / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic_rl_iteration_c2.json"
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
-
-    # ---- e2e through the reference ABI with pinned host buffers
+            "ms": round(pms, 5), "bytes_per_voxel": pass_bytes[i],
+            "gbs": round(pass_bytes[i] * vox / (pms * 1e-3) / 1e9, 1) if pms > 0 else None}
+    # e2e through the reference ABI: pinned host buffers, then pageable
     h_raw = torch.from_numpy(raw).pin_memory()
     h_out = torch.empty((onz, ony, onx), dtype=torch.float32).pin_memory()
     u16p = ctypes.POINTER(ctypes.c_ushort)
     f32p = ctypes.POINTER(ctypes.c_float)
-    rawp = ctypes.cast(ctypes.c_void_p(h_raw.data_ptr()), u16p)
-    outp = ctypes.cast(ctypes.c_void_p(h_out.data_ptr()), f32p)
-
-    def e2e_step():
-        ok = L.RL_interface(rawp, nx, ny, nz, outp, None, w["background"], False, False, n_iters,
-                            0, 0, 0, 0.0, False, False)
-        if ok != 1:
-            raise RuntimeError(L.cdx_last_error().decode())
-
-    e2e_step()
-    if pg:
-        pg.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_s = max_over_ranks(e2e_s, pg, dev)
-    e2e_val = world * vox_iters / e2e_s
-
-    # ---- the same call with pageable numpy buffers, as a ctypes caller such
-    # as pycudadecon passes them
+    bufs = {"pinned": (ctypes.cast(ctypes.c_void_p(h_raw.data_ptr()), u16p),
+                       ctypes.cast(ctypes.c_void_p(h_out.data_ptr()), f32p))}
     p_raw = np.ascontiguousarray(raw)
     p_out = np.empty((onz, ony, onx), np.float32)
-    prawp = p_raw.ctypes.data_as(u16p)
-    poutp = p_out.ctypes.data_as(f32p)
+    bufs["pageable"] = (p_raw.ctypes.data_as(u16p), p_out.ctypes.data_as(f32p))
+    e2e = {}
+    for kind, (rp, op) in bufs.items():
+        def e2e_step():
+            ok = L.RL_interface(rp, nx, ny, nz, op, None, w["background"], False, False, n_iters,
+                                0, 0, 0, 0.0, False, False)
+            if ok != 1:
+                raise RuntimeError(L.cdx_last_error().decode())
+        e2e_step()
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            e2e_step()
+        e2e[kind] = (time.perf_counter() - t0) / steps
+    finite = bool(torch.isfinite(d_out).all().item())
+    launches = int(L.cdx_last_launch_count())
+    cdx.rl_cleanup()
+    td.cleanup()
+    hbm, _ = peaks()
+    achieved = ALG_BYTES_PER_VOXEL_ITER * vox / (iter_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic_rl_iteration_c2.json"
+    if tfile.exists():
+        traffic = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
+    return {"workload": w["name"], "decon_grid_zyx": [gz, gy, gx], "iterations": n_iters,
+            "value": vox * n_iters / (ms * 1e-3), "ms_per_step": ms, "iteration_ms": iter_ms,
+            "iteration_ms_profiled": it_ms.value / max(it_n.value, 1), "prepost_ms": prepost,
+            "e2e": {"value": vox * n_iters / e2e["pinned"], "host_buffers": "pinned",
+                    "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": int(p_out.nbytes),
+                    "pageable": {"value": vox * n_iters / e2e["pageable"],
+                                 "ms_per_step": 1e3 * e2e["pageable"],
+                                 "host_buffers": "pageable numpy arrays"}},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic,
+                         "kernel": "one RL iteration (9 fused passes and the lambda kernel)",
+                         "passes": passes},
+            "launches_per_step": launches, "output_finite": finite}
 
-    def e2e_pageable_step():
-        ok = L.RL_interface(prawp, nx, ny, nz, poutp, None, w["background"], False, False,
-                            n_iters, 0, 0, 0, 0.0, False, False)
-        if ok != 1:
-            raise RuntimeError(L.cdx_last_error().decode())
 
-    e2e_pageable_step()
+def measure_grid3(cdx, torch, dev, steps):
+    """128x512x1024, 20 iterations, both forms (device-resident)."""
+    from cudadecon_gb300 import synth
+    L = cdx.lib()
+    shape = GRID3["shape"]
+    nz, ny, nx = shape
+    td = tempfile.TemporaryDirectory()
+    tab = synth.gaussian_otf_table(129, 64, 1.5, 4.0)
+    p = Path(td.name) / "otf.tif"
+    synth.write_otf(p, tab)
+    cdx.rl_init(shape, p, dr=0.1, dz=0.2, dr_psf=0.1, dz_psf=0.2)
+    raw = synth.bead_stack_gpu(shape, n_beads=4000, psf_sigma_xy=1.5, psf_sigma_z=4.0,
+                               seed=GRID3["seed"])
+    out = torch.empty(shape, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    n = GRID3["n_iters"]
+    res = {}
+    for form, code in (("plain", 0), ("mixed", 1)):
+        L.cdx_set_dft_form(code)
+
+        def step(iters=n):
+            ok = L.cdx_RL_device(ctypes.c_void_p(raw.data_ptr()), nx, ny, nz,
+                                 ctypes.c_void_p(out.data_ptr()), None, 100.0, False, False,
+                                 iters, 0, 0, 0, 0.0, False, False, sp)
+            if ok != 1:
+                raise RuntimeError(L.cdx_last_error().decode())
+
+        with torch.cuda.stream(stream):
+            step()
+        ms = events_ms(torch, stream, step, steps)
+        pre = events_ms(torch, stream, lambda: step(0), steps)
+        res[form] = {"value": nz * ny * nx * n / (ms * 1e-3), "ms_per_step": ms,
+                     "iteration_ms": (ms - pre) / n, "tc_status_ok": bool(L.cdx_tc_status())}
+    L.cdx_set_dft_form(0)
+    cdx.rl_cleanup()
+    td.cleanup()
+    res["mixed_over_plain"] = res["mixed"]["value"] / res["plain"]["value"]
+    res["workload"] = f"{nz}x{ny}x{nx}, {n} RL it, Gaussian OTF"
+    return res
+
+
+def measure_timelapse(cdx, torch, dev, steps):
+    """8 timepoints x 2 channels of 256x1024x1024 u16: camcor, deskew, 20
+    iterations, rotate, one OTF per channel (RL_interface_init per channel and
+    step, as a caller switching channels does).  Device-resident raw stacks."""
+    from cudadecon_gb300 import synth
+    L = cdx.lib()
+    w = LAPSE
+    nz, ny, nx = w["shape"]
+    td = tempfile.TemporaryDirectory()
+    otfs = []
+    for c, (sxy, sz) in enumerate(((1.3, 3.0), (1.5, 3.4))):
+        p = Path(td.name) / f"otf{c}.tif"
+        synth.write_otf(p, synth.gaussian_otf_table(129, 64, sxy, sz))
+        otfs.append(p)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(w["seed"])
+    raws = []
+    for _ in range(w["timepoints"] * w["channels"]):
+        lam = 100.0 + 3000.0 * (torch.rand(w["shape"], generator=gen, device=dev) < 2e-4).float()
+        raws.append(torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32)
+                    .to(torch.uint16))
+        del lam
+    cam = torch.from_numpy(synth.camcor_params(ny, nx, seed=w["seed"])).to(dev)
+    cc = torch.empty(w["shape"], dtype=torch.uint16, device=dev)
+    kw = dict(dr=w["dr"], dz=w["dz"], dr_psf=w["dr"], dz_psf=0.2, deskew_angle=w["angle"],
+              rotation_angle=w["angle"])
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    state = {}
+
+    def step():
+        for c in range(w["channels"]):
+            cdx.rl_init(w["shape"], otfs[c], **kw)
+            if "out" not in state:
+                state["out"] = torch.empty(cdx.output_shape(), dtype=torch.float32, device=dev)
+                state["grid"] = cdx.decon_grid()
+            out = state["out"]
+            for t in range(w["timepoints"]):
+                r = raws[t * w["channels"] + c]
+                if L.cdx_camcor_device(ctypes.c_void_p(r.data_ptr()), nx, ny, nz,
+                                       ctypes.c_void_p(cam.data_ptr()),
+                                       ctypes.c_void_p(cc.data_ptr()), sp) != 1:
+                    raise RuntimeError(L.cdx_last_error().decode())
+                if L.cdx_RL_device(ctypes.c_void_p(cc.data_ptr()), nx, ny, nz,
+                                   ctypes.c_void_p(out.data_ptr()), None, 100.0, False, False,
+                                   w["n_iters"], 0, 0, 0, 0.0, False, False, sp) != 1:
+                    raise RuntimeError(L.cdx_last_error().decode())
+
+    step()
+    stream.synchronize()
+    ms = events_ms(torch, stream, step, steps)
+    gz, gy, gx = state["grid"]
+    vox = gz * gy * gx * w["timepoints"] * w["channels"]
+    finite = bool(torch.isfinite(state["out"]).all().item())
+    cdx.rl_cleanup()
+    td.cleanup()
+    hbm, _ = peaks()
+    v = vox * w["n_iters"] / (ms * 1e-3)
+    return {"workload": f"{w['timepoints']} timepoints x {w['channels']} channels of "
+                        f"{nz}x{ny}x{nx} u16, camcor, deskew {w['angle']} deg -> {gz}x{gy}x{gx}, "
+                        f"{w['n_iters']} RL it, rotate, 2 OTFs",
+            "value": v, "unit": "voxel-iter/s", "ms_per_step": ms,
+            "roofline_frac": ALG_BYTES_PER_VOXEL_ITER * v / 1e9 / hbm, "output_finite": finite}
+
+
+def run_gb300(args):
+    import torch
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    import cudadecon_gb300 as cdx
+    L = cdx.lib()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    stacks = batch_inputs(dev)
+    # ---- headline: the batch, plain FP32 form
+    clk = ClockSampler(local)
+    clk.start()
+    # warm-up (graph capture, plans) before the barrier
+    measure_batch(cdx, torch, dev, stream, stacks, 1, args.warmup, 0)
     if pg:
         pg.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_pageable_step()
-    e2e_pg_s = max_over_ranks((time.perf_counter() - t0) / args.steps, pg, dev)
-
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    ms, vox_iters, launches, finite = measure_batch(cdx, torch, dev, stream, stacks, args.steps,
+                                                    0, 0)
+    t_wall1 = time.time()
+    clocks = clk.stop(t_wall0, t_wall1)
+    ms = max_over_ranks(ms, pg, dev)
+    value = world * vox_iters / (ms * 1e-3)
+    # ---- the mixed-precision form on the same batch
+    ms_mixed, _, launches_mixed, finite_mixed = measure_batch(cdx, torch, dev, stream, stacks,
+                                                              args.steps, args.warmup, 1)
+    ms_mixed = max_over_ranks(ms_mixed, pg, dev)
+    value_mixed = world * vox_iters / (ms_mixed * 1e-3)
+    # ---- e2e (host buffers)
+    e2e_s, h2d, d2h = measure_batch_e2e(cdx, torch, dev, stream, stacks,
+                                        max(1, min(args.steps, 5)))
+    e2e_s = max_over_ranks(e2e_s, pg, dev)
+    L.cdx_batch_release()
+    del stacks
+    torch.cuda.empty_cache()
+    hbm, peak_kind = peaks()
+    achieved = ALG_BYTES_PER_VOXEL_ITER * vox_iters / (ms * 1e-3) / 1e9
+    secondary = {}
+    if not args.no_secondary:
+        secondary["stage_scan"] = measure_stage_scan(cdx, torch, dev, args.steps, pg)
+        secondary["grid_128x512x1024"] = measure_grid3(cdx, torch, dev, max(3, args.steps // 4))
+        torch.cuda.empty_cache()
+        if not args.no_timelapse:
+            secondary["timelapse"] = measure_timelapse(cdx, torch, dev, 2)
+            torch.cuda.empty_cache()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_leg(raw, tab)
-
-    batch = None
-    if rank == 0 and not args.no_batch:
-        batch = run_batch(cdx, dev)
-
+        cpu = cpu_baseline_leg()
     if rank == 0:
         line = {
             "metric": "RL voxel-iterations/s", "value": value, "unit": "voxel-iter/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded beads + filaments)",
-            "config": {"workload": WORKLOAD["name"], "decon_grid_zyx": [gz, gy, gx],
-                       "iterations": n_iters, "form": "plain FP32",
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Poisson background "
+                                                         "+ sparse beads, generated on the GPU)",
+            "config": {"workload": BATCH_NAME, "stacks": BATCH["stacks"],
+                       "decon_voxels": vox_iters // BATCH["iterations"],
+                       "iterations": BATCH["iterations"], "form": "plain FP32",
                        "parallelism": f"replicas x{world}",
-                       "l2_policy": "working set ~0.45 GB > 129 MB L2 (no flush needed)"},
-            "e2e": {"value": e2e_val, "unit": "voxel-iter/s",
-                    "h2d_bytes_per_step": int(raw.nbytes), "d2h_bytes_per_step": int(h_out.numel() * 4),
-                    "host_buffers": "pinned",
-                    "pageable": {"value": world * vox_iters / e2e_pg_s, "unit": "voxel-iter/s",
-                                 "ms_per_step": 1e3 * e2e_pg_s,
-                                 "host_buffers": "pageable numpy arrays"}},
+                       "l2_policy": "working set ~10 GB > 129 MB L2 (no flush needed)"},
+            "forms": {"plain": {"value": value, "ms_per_step": ms},
+                      "mixed": {"value": value_mixed, "ms_per_step": ms_mixed,
+                                "what": "x-pass DFT stages of rows with a tensor-core plan "
+                                        "(256, 512, 756, 1024) as tcgen05 MMAs in split TF32"},
+                      "mixed_over_plain": value_mixed / value},
+            "e2e": {"value": world * vox_iters / e2e_s, "unit": "voxel-iter/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "host_buffers": "pinned"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": traffic,
-                         "nominal_gbs": NOMINAL_HBM_GBS, "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
-                         "kernel": "one RL iteration (9 fused passes and the lambda kernel)",
+                         "frac": achieved / hbm, "traffic": None,
+                         "nominal_gbs": NOMINAL_HBM_GBS,
+                         "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
+                         "kernel": "one batch call: every stack's RL iterations (9 fused passes "
+                                   "and the lambda kernel each) and conditioning",
                          "alg_bytes_per_voxel_iter": ALG_BYTES_PER_VOXEL_ITER,
-                         "iteration_ms": iter_ms, "iteration_ms_profiled": iter_ms_profiled,
-                         "prepost_ms_per_step": prepost_ms,
-                         "peak_source": f"{peak_kind} hbm_gbs",
-                         "passes": passes},
+                         "peak_source": f"{peak_kind} hbm_gbs"},
             "cpu_baseline": cpu,
             "clocks": clocks,
-            "gpu_launches": launches_per_step * args.steps,
-            "output_finite": finite,
-            "batch": batch,
+            "gpu_launches": launches * args.steps,
+            "output_finite": finite and finite_mixed,
+            "secondary": secondary,
         }
         print(json.dumps(line), flush=True)
-    td.cleanup()
     return 0
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batch", action="store_true",
-                    help="skip the batched uneven-stacks measurement")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="only the batched headline workload")
+    ap.add_argument("--no-timelapse", action="store_true",
+                    help="skip the 16-stack time-lapse secondary workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

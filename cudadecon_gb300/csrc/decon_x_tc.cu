@@ -74,7 +74,7 @@ struct TcPlan {
   static constexpr unsigned BYTES = MB + 64;  // mbarriers, TMEM slot, flags
   // CTAs per SM the launch bounds ask for (shared memory allows this many)
   static constexpr int MINB_ = (int)((228u * 1024u) / (BYTES + 1024u));
-  static constexpr int MINB = MINB_ < 1 ? 1 : (MINB_ > 3 ? 3 : MINB_);
+  static constexpr int MINB = MINB_ < 1 ? 1 : (MINB_ > 2 ? 2 : MINB_);
   // exchange tile (natural order, P rows of LX float2) aliases this
   // warpgroup's A
   static constexpr int LX = L + 8;
@@ -242,20 +242,24 @@ __device__ __forceinline__ void tc_inverse(TcWg& w, unsigned char* sm, const flo
     const int p = t % P, n2 = t / P;
     const int ya = y0 + 2 * p;
     const long long zo = (long long)z * g.nyp + ya;
+    // every load of the vector first (the stores into A would otherwise
+    // keep the compiler from moving later loads ahead of them)
+    float2 v[Q0];
 #pragma unroll
-    for (int n1 = 0; n1 < Q0; ++n1) {
-      const float2 v = ya < g.ny ? packed_spec_g(S, g, zo, Q1 * n1 + n2) : make_float2(0.f, 0.f);
-      a_put<TP>(w, t, n1, conj2(v));
-    }
+    for (int n1 = 0; n1 < Q0; ++n1)
+      v[n1] = ya < g.ny ? packed_spec_g(S, g, zo, Q1 * n1 + n2) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int n1 = 0; n1 < Q0; ++n1) a_put<TP>(w, t, n1, conj2(v[n1]));
   }
   tc_stage<TP, TP::KP0, TP::NP0>(w, sm, TP::B0, d);
   if (t < P * Q1) {
     const int p = t % P, n2 = t / P;
+    float2 c[Q0];
 #pragma unroll
-    for (int k1 = 0; k1 < Q0; ++k1) {
-      const float2 v = cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), tw[n2 * TP::TWS + k1]);
-      a_put<TP>(w, k1 * P + p, n2, v);
-    }
+    for (int k1 = 0; k1 < Q0; ++k1) c[k1] = tw[n2 * TP::TWS + k1];
+#pragma unroll
+    for (int k1 = 0; k1 < Q0; ++k1)
+      a_put<TP>(w, k1 * P + p, n2, cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), c[k1]));
   }
   tc_stage<TP, TP::KP1, TP::NP1>(w, sm, TP::B1, d);
 #pragma unroll
@@ -277,11 +281,12 @@ __device__ __forceinline__ void tc_forward_rest(TcWg& w, unsigned char* sm, unsi
   tc_stage<TP, KPA, NPA>(w, sm, BA, d);
   if (t < P * QB) {
     const int p = t % P, n2 = t / P;
+    float2 c[QA];
 #pragma unroll
-    for (int k1 = 0; k1 < QA; ++k1) {
-      const float2 c = TWT ? tw[k1 * TP::TWS + n2] : tw[n2 * TP::TWS + k1];
-      a_put<TP>(w, k1 * P + p, n2, cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), c));
-    }
+    for (int k1 = 0; k1 < QA; ++k1) c[k1] = TWT ? tw[k1 * TP::TWS + n2] : tw[n2 * TP::TWS + k1];
+#pragma unroll
+    for (int k1 = 0; k1 < QA; ++k1)
+      a_put<TP>(w, k1 * P + p, n2, cmul(make_float2(d[2 * k1], d[2 * k1 + 1]), c[k1]));
   }
   tc_stage<TP, KPB, NPB>(w, sm, BB, d);
   // the last MMA has read A: the exchange tile may overwrite it
@@ -339,25 +344,26 @@ k_xtc_fwd(Geom g, const float4* btab, const float4* twtab, const float* X, float
       const int ya = y0 + 2 * p;
       const long long o = ((long long)z * g.ny + ya) * g.nx;
       const bool va = ya < g.ny, vb = ya + 1 < g.ny;
+      // loads first, then the prediction, its stores and the A rows
+      float2 xv[Q0], mv[Q0];
 #pragma unroll
       for (int n1 = 0; n1 < Q0; ++n1) {
-        const int e = Q1 * n1 + n2;
-        float a = 0.f, b = 0.f;
-        if (va) {
-          a = X[o + e];
-          if (predict) {
-            a = predict_y(a, Xm1[o + e], lamv);
-            __stcs(Xm1 + o + e, a);
-          }
+        const long long i = o + Q1 * n1 + n2;
+        xv[n1] = make_float2(va ? __ldcs(X + i) : 0.f, vb ? __ldcs(X + i + g.nx) : 0.f);
+        if (predict)
+          mv[n1] = make_float2(va ? __ldcs(Xm1 + i) : 0.f, vb ? __ldcs(Xm1 + i + g.nx) : 0.f);
+      }
+#pragma unroll
+      for (int n1 = 0; n1 < Q0; ++n1) {
+        const long long i = o + Q1 * n1 + n2;
+        float2 yv = xv[n1];
+        if (predict) {
+          yv.x = predict_y(yv.x, mv[n1].x, lamv);
+          yv.y = predict_y(yv.y, mv[n1].y, lamv);
+          if (va) __stcs(Xm1 + i, yv.x);
+          if (vb) __stcs(Xm1 + i + g.nx, yv.y);
         }
-        if (vb) {
-          b = X[o + g.nx + e];
-          if (predict) {
-            b = predict_y(b, Xm1[o + g.nx + e], lamv);
-            __stcs(Xm1 + o + g.nx + e, b);
-          }
-        }
-        a_put<TP>(w, t, n1, make_float2(a, b));
+        a_put<TP>(w, t, n1, yv);
       }
     }
     tc_forward_rest<TP, Q0, Q1, TP::KP0, TP::NP0, TP::KP1, TP::NP1, false>(w, sm, TP::B0, TP::B1,
@@ -394,12 +400,17 @@ k_xtc_ratio(Geom g, const float4* btab, const float4* twtab, float2* S, const fl
       const int ya = y0 + 2 * p;
       const long long o = ((long long)z * g.ny + ya) * g.nx;
       const bool va = ya < g.ny, vb = ya + 1 < g.ny;
+      float2 rv[Q1];
 #pragma unroll
       for (int k2 = 0; k2 < Q1; ++k2) {
-        const int e = k1 + Q0 * k2;
+        const long long i = o + k1 + Q0 * k2;
+        rv[k2] = make_float2(va ? __ldcs(raw + i) : 0.f, vb ? __ldcs(raw + i + g.nx) : 0.f);
+      }
+#pragma unroll
+      for (int k2 = 0; k2 < Q1; ++k2) {
         float2 r = make_float2(0.f, 0.f);
-        if (va) r.x = rl_ratio(d[2 * k2], __ldcs(raw + o + e), eps);
-        if (vb) r.y = rl_ratio(d[2 * k2 + 1], __ldcs(raw + o + g.nx + e), eps);
+        if (va) r.x = rl_ratio(d[2 * k2], rv[k2].x, eps);
+        if (vb) r.y = rl_ratio(d[2 * k2 + 1], rv[k2].y, eps);
         a_put<TP>(w, t, k2, r);
       }
     }
@@ -438,18 +449,24 @@ k_xtc_update(Geom g, const float4* btab, const float4* twtab, const float2* S, c
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
         if (ya + r >= g.ny) break;
-        const long long o = ((long long)z * g.ny + ya + r) * g.nx;
+        const long long o = ((long long)z * g.ny + ya + r) * g.nx + k1;
+        // the row's loads first (Xout may alias Y, so a store would keep
+        // later loads behind it)
+        float yv[Q1], gv[Q1];
 #pragma unroll
         for (int k2 = 0; k2 < Q1; ++k2) {
-          const long long i = o + k1 + Q0 * k2;
-          const float yv = __ldcs(Y + i);
-          float xn = __fmul_rn(d[2 * k2 + r], yv);
+          yv[k2] = __ldcs(Y + o + Q0 * k2);
+          gv[k2] = dots ? __ldcs(G + o + Q0 * k2) : 0.f;
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < Q1; ++k2) {
+          const long long i = o + Q0 * k2;
+          float xn = __fmul_rn(d[2 * k2 + r], yv[k2]);
           xn = xn > 0.f ? xn : 0.f;
-          const float gn = __fsub_rn(xn, yv);
+          const float gn = __fsub_rn(xn, yv[k2]);
           if (dots) {
-            const float go = __ldcs(G + i);
-            acc_add(acc[0], acc[1], __fmul_rn(gn, go));
-            acc_add(acc[2], acc[3], __fmul_rn(go, go));
+            acc_add(acc[0], acc[1], __fmul_rn(gn, gv[k2]));
+            acc_add(acc[2], acc[3], __fmul_rn(gv[k2], gv[k2]));
           }
           Xout[i] = xn;
           __stcs(G + i, gn);
@@ -581,14 +598,16 @@ void tc_tables_free(TcTables& t) {
   t = TcTables{};
 }
 
-// Persistent grid: as many CTAs as fit on the device at once, at most one
-// per tile group.
-template <class K>
-static int tc_grid(K kern, size_t smem, int tiles, int wg, int* grid) {
-  int dev = 0, sms = 0, per = 0;
+// Persistent grid: as many CTAs as fit on the device at once (the launch
+// bounds' CTAs per SM, or fewer when shared memory holds fewer), at most one
+// per group of WG tiles.
+static int tc_grid(unsigned smem, int minb, int tiles, int wg, int* grid) {
+  int dev = 0, sms = 0, smem_sm = 0;
   CDX_CHECK(cudaGetDevice(&dev));
   CDX_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  CDX_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 128 * wg, smem));
+  CDX_CHECK(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  int per = smem_sm / (int)(smem + 1024);
+  if (per > minb) per = minb;
   if (per < 1) {
     set_error("tc_grid", "tensor-core kernel does not fit an SM");
     return cudaErrorInvalidConfiguration;
@@ -607,7 +626,7 @@ static int tc_fwd_go(const Geom& g, const TcTables& t, const float* X, float* Xm
   if (int rc = smem_optin(kern, smem)) return rc;
   const int tiles = ceil_div(g.ny, 2 * TP::P) * g.nz;
   int grid = 0;
-  if (int rc = tc_grid(kern, smem, tiles, TP::WG, &grid)) return rc;
+  if (int rc = tc_grid(TP::BYTES, TP::MINB, tiles, TP::WG, &grid)) return rc;
   CDX_CHECK(launch_pdl(kern, dim3(grid), dim3(128 * TP::WG), smem, st, g,
                        (const float4*)t.d_b, (const float4*)t.d_tw, X, Xm1, lam, predict, S, err));
   CDX_LAUNCH_CHECK("k_xtc_fwd");
@@ -622,7 +641,7 @@ static int tc_ratio_go(const Geom& g, const TcTables& t, float2* S, const float*
   if (int rc = smem_optin(kern, smem)) return rc;
   const int tiles = ceil_div(g.ny, 2 * TP::P) * g.nz;
   int grid = 0;
-  if (int rc = tc_grid(kern, smem, tiles, TP::WG, &grid)) return rc;
+  if (int rc = tc_grid(TP::BYTES, TP::MINB, tiles, TP::WG, &grid)) return rc;
   CDX_CHECK(launch_pdl(kern, dim3(grid), dim3(128 * TP::WG), smem, st, g,
                        (const float4*)t.d_b, (const float4*)t.d_tw, S, raw, eps, err));
   CDX_LAUNCH_CHECK("k_xtc_ratio");
@@ -638,7 +657,7 @@ static int tc_update_go(const Geom& g, const TcTables& t, const float2* S, const
   if (int rc = smem_optin(kern, smem)) return rc;
   const int tiles = ceil_div(g.ny, 2 * TP::P) * g.nz;
   int grid = 0;
-  if (int rc = tc_grid(kern, smem, tiles, TP::WG, &grid)) return rc;
+  if (int rc = tc_grid(TP::BYTES, TP::MINB, tiles, TP::WG, &grid)) return rc;
   if (dots && grid > w.max_blocks) {
     set_error("launch_x_inv_update", "partials buffer too small");
     return cudaErrorInvalidValue;

@@ -106,12 +106,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, unsigned parity, long 
   const long long t0 = clock64();
   while (true) {
     unsigned done;
+    // the thread may sleep in the instruction (up to the 20 us hint) until
+    // the phase completes, instead of spinning
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(20000u)
         : "memory");
     if (done) return true;
     if (clock64() - t0 > max_cycles) return false;

@@ -54,7 +54,8 @@ def _load():
                                    ctypes.c_int, _fp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_float, ctypes.c_float, ctypes.c_float, _fp,
                                    ctypes.c_int, ctypes.c_int]
-    L.ref_session_step.argtypes = [_vp, ctypes.c_float, ctypes.c_int, _vp]
+    L.ref_session_step.argtypes = [ctypes.c_int, _vp, ctypes.c_float, ctypes.c_int, _vp]
+    L.ref_session_close.argtypes = [ctypes.c_int]
     L.ref_session_close.restype = None
     if L.ref_load(str(REF).encode()) != 1:
         _why = "ref_load failed: " + L.ref_last_error().decode()
@@ -177,17 +178,20 @@ class Session:
         self.raw_shape = (nz, ny, nx)
         self.grid = (nz, ny, gx)
         self.out_shape = (nzr, ny, nxr)
-        _check(L.ref_session_open(nx, ny, nz, float(state.deskewFactor), int(gx),
-                                  self._otf.ctypes.data_as(_fp), nxo, nyo, nzo, float(kxs),
-                                  float(kys), float(kzs),
-                                  rot.ctypes.data_as(_fp) if rot is not None else None,
-                                  int(nxr), int(nzr)), "ref_session_open")
+        self.h = L.ref_session_open(nx, ny, nz, float(state.deskewFactor), int(gx),
+                                    self._otf.ctypes.data_as(_fp), nxo, nyo, nzo, float(kxs),
+                                    float(kys), float(kzs),
+                                    rot.ctypes.data_as(_fp) if rot is not None else None,
+                                    int(nxr), int(nzr))
+        if self.h < 0:
+            raise RuntimeError(f"ref_session_open: {L.ref_last_error().decode()}")
 
     def step(self, d_raw, background, n_iters, d_out):
-        _check(_load().ref_session_step(d_raw.data_ptr(), float(background), int(n_iters),
-                                        d_out.data_ptr()), "ref_session_step")
+        _check(_load().ref_session_step(self.h, d_raw.data_ptr(), float(background),
+                                        int(n_iters), d_out.data_ptr()), "ref_session_step")
 
     def close(self):
         L = _load()
-        if L is not None:
-            L.ref_session_close()
+        if L is not None and self.h >= 0:
+            L.ref_session_close(self.h)
+            self.h = -1

@@ -370,6 +370,8 @@ namespace {
 struct RefSession {
   bool open = false;
   int nx_raw = 0, ny = 0, nz = 0, nx = 0;  // raw grid and deskewed (decon) width
+  int nxotf = 0, nyotf = 0, nzotf = 0;
+  float kxs = 0.f, kys = 0.f, kzs = 0.f;
   double deskew = 0.0;
   int nx_rot = 0, nz_rot = 0;
   size_t N = 0, M = 0, Nraw = 0;
@@ -384,31 +386,53 @@ struct RefSession {
   std::vector<double> hpart, hsum;
   std::vector<unsigned> hcnt;
 };
-RefSession g_s;
+std::vector<RefSession> g_sessions;
 
-void session_free() {
-  if (g_s.pf) cufftDestroy(g_s.pf);
-  if (g_s.pi) cufftDestroy(g_s.pi);
-  void* bufs[] = {g_s.rawotf, g_s.otf, g_s.fft, g_s.X0,   g_s.X,      g_s.CC,      g_s.rawb,
-                  g_s.Xm1,    g_s.Y,   g_s.G1,  g_s.G2,   g_s.rot,    g_s.part,    g_s.intres,
-                  g_s.counter};
+void session_free(RefSession& s) {
+  if (s.pf) cufftDestroy(s.pf);
+  if (s.pi) cufftDestroy(s.pi);
+  void* bufs[] = {s.rawotf, s.otf, s.fft, s.X0,   s.X,      s.CC,      s.rawb,
+                  s.Xm1,    s.Y,   s.G1,  s.G2,   s.rot,    s.part,    s.intres,
+                  s.counter};
   for (void* b : bufs)
     if (b) cudaFree(b);
-  g_s = RefSession{};
+  s = RefSession{};
+}
+
+RefSession* session(int h) {
+  if (h < 0 || h >= (int)g_sessions.size() || !g_sessions[h].open) {
+    g_err = "no such session";
+    return nullptr;
+  }
+  return &g_sessions[h];
 }
 }  // namespace
 
-void ref_session_close(void) { session_free(); }
+void ref_session_close(int h) {
+  if (h >= 0 && h < (int)g_sessions.size()) session_free(g_sessions[h]);
+}
 
 // nx_raw, ny, nz: the cropped raw grid; deskewFactor / nx_desk as
 // RL_interface_init computes them (nx_desk = nx_raw when deskewFactor is 0);
 // rot4: the rotation matrix, or NULL for no rotation (then nx_rot, nz_rot
-// are ignored).
+// are ignored).  Returns a session handle (>= 0), or -1.  Each session holds
+// its own buffers, cuFFT plans and OTF array, as one RL_interface_init
+// state of the reference; the constants of the reference kernels are set
+// again by every step.
 int ref_session_open(int nx_raw, int ny, int nz, double deskewFactor, int nx_desk,
                      const float* otf_host, int nxotf, int nyotf, int nzotf, float kxs, float kys,
                      float kzs, const float* rot4, int nx_rot, int nz_rot) {
-  session_free();
-  RefSession& s = g_s;
+  int h = 0;
+  while (h < (int)g_sessions.size() && g_sessions[h].open) ++h;
+  if (h == (int)g_sessions.size()) g_sessions.emplace_back();
+  RefSession& s = g_sessions[h];
+  s = RefSession{};
+  s.nxotf = nxotf;
+  s.nyotf = nyotf;
+  s.nzotf = nzotf;
+  s.kxs = kxs;
+  s.kys = kys;
+  s.kzs = kzs;
   s.nx_raw = nx_raw;
   s.ny = ny;
   s.nz = nz;
@@ -428,7 +452,7 @@ int ref_session_open(int nx_raw, int ny, int nz, double deskewFactor, int nx_des
       !set_const("const_nzotf", &nzotf, 4) || !set_const("const_kxscale", &kxs, 4) ||
       !set_const("const_kyscale", &kys, 4) || !set_const("const_kzscale", &kzs, 4) ||
       !set_const("const_eps", &eps, 4))
-    return 0;
+    return -1;
   const size_t notf = (size_t)nxotf * nyotf * nzotf;
   s.nbDot = (unsigned)ceil(((float)s.N) / 1024 / 2);
   s.nbSum = (unsigned)ceil(s.Nraw / (float)1024 / 2);
@@ -461,22 +485,34 @@ int ref_session_open(int nx_raw, int ny, int nz, double deskewFactor, int nx_des
   s.hsum.resize(s.nbSum);
   s.hcnt.resize(s.nbSum);
   if (!ok) {
-    session_free();
-    return 0;
+    session_free(s);
+    return -1;
   }
   s.open = true;
-  return 1;
+  return h;
+}
+
+// transferConstants for session s (RLgpuImpl.cu:74-91)
+static bool session_constants(const RefSession& s) {
+  const int nx = s.nx, ny = s.ny, nz = s.nz;
+  const unsigned nxyz = (unsigned)s.N;
+  const float eps = std::numeric_limits<float>::epsilon();
+  return set_const("const_nx", &nx, 4) && set_const("const_ny", &ny, 4) &&
+         set_const("const_nz", &nz, 4) && set_const("const_nxyz", &nxyz, 4) &&
+         set_const("const_nxotf", &s.nxotf, 4) && set_const("const_nyotf", &s.nyotf, 4) &&
+         set_const("const_nzotf", &s.nzotf, 4) && set_const("const_kxscale", &s.kxs, 4) &&
+         set_const("const_kyscale", &s.kys, 4) && set_const("const_kzscale", &s.kzs, 4) &&
+         set_const("const_eps", &eps, 4);
 }
 
 // One call: raw (device, the cropped (nz, ny, nx_raw) stack as float, which
 // the reference converts on the host) -> out (device, the rotated result, or
 // the deskewed decon grid without rotation).  Returns after the device work.
-int ref_session_step(const float* d_raw, float background, int nIter, float* d_out) {
-  RefSession& s = g_s;
-  if (!s.open) {
-    g_err = "session not open";
-    return 0;
-  }
+int ref_session_step(int h, const float* d_raw, float background, int nIter, float* d_out) {
+  RefSession* sp = session(h);
+  if (!sp) return 0;
+  RefSession& s = *sp;
+  if (!session_constants(s)) return 0;
   const size_t N = s.N, M = s.M;
   const float eps = std::numeric_limits<float>::epsilon();
   // X_k <- raw (the reference's H2D), backgroundSubtraction_GPU (RLgpuImpl.cu:134-154)
