@@ -39,6 +39,42 @@ struct OtfColMulStore {
   }
 };
 
+// Runtime-width interleaved tile of W columns: element e of column v at
+// sm[e * W + v] (the staged input of the generic z pass).
+struct ColIOr {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  float2* sm;
+  int W;
+  __device__ __forceinline__ float2 ld(int v, int e) const { return sm[e * W + v]; }
+};
+
+// Last forward stage of the generic z pass: multiply element e (= kz) of
+// column v by the OTF, interpolated from the kz-resampled radial table at the
+// column's precomputed radius (mode 0: table column cir[v], fraction car[v];
+// -1 outside the table) or read from the 3D array (mode 1), conjugated when
+// conj; same arithmetic as OtfColMulStore.
+struct OtfColMulStoreG {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  SmemIO io;
+  const float4* tz;
+  const float2* full;  // mode 1: the plane's column y0
+  const int* cir;
+  const float* car;
+  int nr, nyp, ncols, mode, conj;
+  __device__ __forceinline__ void st(int v, int e, float2 x) const {
+    float2 o = make_float2(0.f, 0.f);
+    if (mode == 1) {
+      if (v < ncols) o = __ldg(full + (long long)e * nyp + v);
+    } else {
+      const int ir = cir[v];
+      if (ir >= 0) o = otf_lerp(__ldg(tz + (long long)e * nr + ir), car[v]);
+    }
+    io.st(v, e, conj ? cmulconj(x, o) : cmul(x, o));
+  }
+};
+
 // MODE and CONJ: the OTF mode and the conjugation as compile-time constants
 // (static plans), or -1 to read them from otf.mode and conj (generic engine).
 template <class Run, int MODE, int CONJ>
@@ -94,40 +130,57 @@ k_z_pass(Geom g, FftDev fz, float2* __restrict__ S, OtfDev otf, int conj, int fw
     Run::template run<false>(fz, W, invW, true, stw, io, io, ost);
     Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
   } else {
-    const SmemIO io{smem + nz, W, 1};
-    float2* otf_tile = smem + nz + spad_size(W * nz);
+    // Generic engine: the tile (W columns of nz elements) is copied with
+    // cp.async into an unpadded interleaved stage at the start of the padded
+    // transform tile; the first stage reads it before its barrier, so the
+    // two may alias.  The OTF radius is computed once per column.
+    const int zoff = nz + (nz & 1);
+    const SmemIO io{smem + zoff, W, 1};
+    int* cir = reinterpret_cast<int*>(smem + zoff + spad_size(W * nz));
+    float* car = reinterpret_cast<float*>(cir + W);
+    const float2* src = S + (long long)kx * g.plane + y0;
     load_twiddles(fz, stw);
+    for (int v = threadIdx.x; v < W; v += blockDim.x) {
+      const int y = y0 + v;
+      int ir = -1;
+      float ar = 0.f;
+      if (y < g.ny && otf.mode == 0) {
+        int i = 0;
+        if (otf_radius(otf, kx, y, g.ny, i, ar)) ir = i;
+      }
+      cir[v] = ir;
+      car[v] = ar;
+    }
     grid_dep_wait();
     grid_dep_launch();
+    if ((W & 1) == 0) {
+      // column pairs: 16-byte copies (y0 and the row pitch are even)
+      const int half = W >> 1;
+      for (int idx = threadIdx.x; idx < nz * half; idx += blockDim.x) {
+        int z, c;
+        divmod_small<0>(idx, half, 1.f / (float)half, z, c);
+        if (y0 + 2 * c < g.ny)
+          cp_async16(io.sm + z * W + 2 * c, src + (long long)z * g.nyp + 2 * c);
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < nz * W; idx += blockDim.x) {
+        int z, c;
+        divmod_small<0>(idx, W, invW, z, c);
+        if (y0 + c < g.ny) cp_async8(io.sm + z * W + c, src + (long long)z * g.nyp + c);
+      }
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    const ColIOr stg{io.sm, W};
     if (fwd_only) {
-      __syncthreads();
-      Run::template run<false>(fz, W, invW, true, stw, io, gio, gio);
+      Run::template run<false>(fz, W, invW, true, stw, io, stg, gio);
       return;
     }
-    // OTF of every (y, z) of the tile, interpolated on the fly from the
-    // kz-resampled radial table (dev_otfinterpolate RA branch,
-    // RLgpuImpl.cu:238-273: kr = sqrt(kx^2 + ky^2), zero at kr >= nr-1) or
-    // read from the precomputed 3D array
-    for (int idx = threadIdx.x; idx < W * nz; idx += blockDim.x) {
-      int w, z;
-      divmod_small<Run::kV>(idx, W, invW, z, w);
-      const int y = y0 + w;
-      float2 o = make_float2(0.f, 0.f);
-      if (y < g.ny) {
-        if (otf.mode == 1) {
-          o = __ldg(otf.full + (long long)kx * g.plane + (long long)z * g.nyp + y);
-        } else {
-          int ir = 0;
-          float ar = 0.f;
-          if (otf_radius(otf, kx, y, g.ny, ir, ar))
-            o = otf_lerp(__ldg(otf.tz + (long long)z * otf.nr + ir), ar);
-        }
-      }
-      otf_tile[idx] = o;
-    }
-    __syncthreads();
-    const OtfMulStore ost{io, otf_tile, W, conj};
-    Run::template run<false>(fz, W, invW, true, stw, io, gio, ost);
+    const float2* full = otf.mode == 1 ? otf.full + (long long)kx * g.plane + y0 : nullptr;
+    const OtfColMulStoreG ost{io, otf.tz, full, cir, car, otf.nr, g.nyp, g.ny - y0, otf.mode,
+                              conj};
+    Run::template run<false>(fz, W, invW, true, stw, io, stg, ost);
     Run::template run<true>(fz, W, invW, true, stw, io, io, gio);
   }
 }
@@ -136,10 +189,11 @@ template <class Run, int MODE, int CONJ>
 static int z_go(const Geom& g, const FftDev& f, float2* S, const OtfDev& otf, bool conj,
                 bool fwd_only, int W, int T, cudaStream_t st) {
   dim3 grid(ceil_div(g.ny, W), g.nxh);
-  // static: twiddles + unpadded tile; generic: twiddles + padded tile + OTF tile
+  // static: twiddles + unpadded tile; generic: twiddles + padded tile +
+  // per-column OTF radius (index and fraction)
   size_t smem = Run::kStatic
                     ? sizeof(float2) * ((size_t)(g.nz + (g.nz & 1)) + (size_t)W * g.nz)
-                    : fft_smem(g.nz, (long long)W * g.nz, (long long)W * g.nz);
+                    : sizeof(float2) * ((size_t)(g.nz + (g.nz & 1)) + spad_size(W * g.nz) + W);
   auto kern = k_z_pass<Run, MODE, CONJ>;
   if (int rc = smem_optin(kern, smem)) return rc;
   CDX_CHECK(launch_pdl(kern, grid, dim3(T), smem, st, g, f, S, otf, conj ? 1 : 0,
