@@ -517,7 +517,7 @@ def measure_stage_scan(cdx, torch, dev, steps, pg):
     hbm, _ = peaks()
     achieved = ALG_BYTES_PER_VOXEL_ITER * vox / (iter_ms * 1e-3) / 1e9
     traffic = None
-    tfile = ROOT / "profiles" / "traffic_rl_iteration_c2.json"
+    tfile = ROOT / "profiles" / "traffic_rl_iteration_stage_scan.json"
     if tfile.exists():
         traffic = json.loads(tfile.read_text()).get("dram_bytes_per_iteration")
     return {"workload": w["name"], "decon_grid_zyx": [gz, gy, gx], "iterations": n_iters,
@@ -642,6 +642,56 @@ def measure_timelapse(cdx, torch, dev, steps):
             "roofline_frac": ALG_BYTES_PER_VOXEL_ITER * v / 1e9 / hbm, "output_finite": finite}
 
 
+def measure_batch_per_stack(cdx, torch, dev, stacks):
+    """The batch's stacks one cdx_RL_device call at a time (RL_interface_init
+    per stack, no CUDA graph): the same kernels as the batch call, launched
+    individually, for profilers that list launches one by one."""
+    from cudadecon_gb300 import synth
+    L = cdx.lib()
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    iters = BATCH["iterations"]
+    vox = 0
+    td = tempfile.TemporaryDirectory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i, d in enumerate(stacks):
+        p = Path(td.name) / f"otf{i}.tif"
+        synth.write_otf(p, d["otf"])
+        nz, ny, nx = d["raw"].shape
+        cdx.rl_init((nz, ny, nx), p, dr=d["dr"], dz=d["dz"], dr_psf=d["dr_psf"], dz_psf=d["dz_psf"])
+        out = torch.empty(cdx.output_shape(), dtype=torch.float32, device=dev)
+        if L.cdx_RL_device(ctypes.c_void_p(d["raw"].data_ptr()), nx, ny, nz,
+                           ctypes.c_void_p(out.data_ptr()), None, d["background"], False, False,
+                           iters, 0, 0, 0, 0.0, False, False, sp) != 1:
+            raise RuntimeError(L.cdx_last_error().decode())
+        vox += int(np.prod(out.shape))
+    torch.cuda.synchronize()
+    s = time.perf_counter() - t0
+    cdx.rl_cleanup()
+    td.cleanup()
+    return {"workload": BATCH_NAME + " (one call per stack, no graph)", "value": vox * iters / s,
+            "unit": "voxel-iter/s", "seconds": s}
+
+
+def run_only(args):
+    """One workload alone (for profiling): prints its JSON result."""
+    import torch
+    import cudadecon_gb300 as cdx
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    if args.only == "stage_scan":
+        r = measure_stage_scan(cdx, torch, dev, args.steps, None)
+    elif args.only == "grid3":
+        r = measure_grid3(cdx, torch, dev, args.steps)
+    elif args.only == "timelapse":
+        r = measure_timelapse(cdx, torch, dev, args.steps)
+    else:
+        r = measure_batch_per_stack(cdx, torch, dev, batch_inputs(dev))
+    print(json.dumps({"only": args.only, **r}), flush=True)
+    return 0
+
+
 def run_gb300(args):
     import torch
     world, rank, local, pg = dist_setup(args)
@@ -740,7 +790,11 @@ def main():
                     help="only the batched headline workload")
     ap.add_argument("--no-timelapse", action="store_true",
                     help="skip the 16-stack time-lapse secondary workload")
+    ap.add_argument("--only", choices=["stage_scan", "grid3", "timelapse", "batch_per_stack"],
+                    help="run one workload alone and print its result (for profiling)")
     args = ap.parse_args()
+    if args.only:
+        return run_only(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)
