@@ -22,7 +22,11 @@ k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
 template <bool INV, class Run>
 static int y_go(const Geom& g, const FftDev& f, float2* S, int V, int T, cudaStream_t st) {
   const long long nrows = (long long)g.nxh * g.nz;
-  size_t smem = fft_smem(g.ny, (long long)V * g.ny);
+  // a two-radix static plan's padded middle layout may exceed the generic
+  // padded tile
+  size_t tile = spad_size(V * g.ny);
+  if (Run::kStatic && (size_t)Run::kTileF2 > tile) tile = Run::kTileF2;
+  size_t smem = sizeof(float2) * ((size_t)g.ny + tile);
   dim3 grid((unsigned)((nrows + V - 1) / V));
   if (int rc = smem_optin(k_y_pass<INV, Run>, smem)) return rc;
   CDX_CHECK(launch_pdl(k_y_pass<INV, Run>, grid, dim3(T), smem, st, g, f, S, V));

@@ -222,6 +222,18 @@ int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf,
                                                        splan_threads<SP##L, WW>(), st);
       CDX_Z_PLANS(CDX_CASE)
 #undef CDX_CASE
+#define CDX_GCASE(L, WW)                                                                       \
+  case L:                                                                                      \
+    if (otf.mode == 0)                                                                         \
+      return conj ? z_go<StaticRunner<SP##L, WW, true>, 0, 1>(g, fz.sdev, S, otf, conj,        \
+                                                             fwd_only, WW,                     \
+                                                             splan_threads<SP##L, WW>(), st)   \
+                  : z_go<StaticRunner<SP##L, WW, true>, 0, 0>(g, fz.sdev, S, otf, conj,        \
+                                                             fwd_only, WW,                     \
+                                                             splan_threads<SP##L, WW>(), st);  \
+    break;
+      CDX_Z_GEN_PLANS(CDX_GCASE)
+#undef CDX_GCASE
       default:
         break;
     }

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "fft_static.cuh"
+#include "static_plans_gen.cuh"
 
 #define CDX_SPLAN_LIST(F) \
   F(32, 8, 4)             \
@@ -21,7 +22,8 @@
   F(512, 32, 16)          \
   F(756, 9, 12, 7)        \
   F(1024, 32, 32)         \
-  F(1620, 15, 12, 9)
+  F(1620, 15, 12, 9)      \
+  CDX_GEN_SPLANS(F)
 
 // Plans for the x ratio and x update passes where they differ from the
 // length's registered plan: F(L, P, radices...).  1024 = 32*32 gives a row
@@ -31,8 +33,10 @@
 #define CDX_XR_PLANS(F) F(1024, 2, 8, 16, 8)
 
 #define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 2) F(1024, 4) F(1620, 2)
-#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 4)
+#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 4) CDX_GEN_Y_PLANS(F)
 #define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
+// generated z plans: instantiated for radially averaged OTFs only
+#define CDX_Z_GEN_PLANS(F) CDX_GEN_Z_PLANS(F)
 
 namespace cdx {
 
@@ -47,7 +51,6 @@ CDX_XR_PLANS(CDX_DEF_XRPLAN)
 #define CDX_FIT_ROWS(L, V) \
   static_assert(splan_rows_fit<SP##L, V>(), "row tile too small for the static plan of length " #L);
 CDX_X_PLANS(CDX_FIT_ROWS)
-CDX_Y_PLANS(CDX_FIT_ROWS)
 #undef CDX_FIT_ROWS
 #define CDX_FIT_XR(L, P, ...) \
   static_assert(splan_rows_fit<SPR##L, P>(), "row tile too small for the x ratio plan of " #L);

@@ -54,7 +54,11 @@ def _oracle_state(oracle, shape_zyx, table, **kw):
                                    (27, 35, 1620),
                                    # every length of the specialised-plan registry on each axis
                                    (128, 128, 128), (32, 512, 1024), (64, 1024, 256),
-                                   (256, 64, 512), (100, 18, 756)])
+                                   (256, 64, 512), (100, 18, 756),
+                                   # generated compile-time plans (y in [128, 512], z in
+                                   # [32, 160]): two radices, three (343 = 7*7*7), odd
+                                   (35, 135, 40), (49, 343, 24), (125, 500, 30),
+                                   (147, 160, 20), (45, 405, 36)])
 def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
     torch = torch_cuda
     nz, ny, nx = shape
@@ -71,6 +75,8 @@ def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
 @pytest.mark.parametrize("shape", [(16, 32, 30), (20, 24, 45), (64, 256, 256), (100, 256, 756),
                                    (128, 128, 128), (32, 512, 1024),
                                    (16, 40, 1620),     # registered x length (deskewed 1024)
+                                   (63, 189, 50),      # generated y and z plans
+                                   (150, 448, 24),
                                    (128, 512, 1024)])  # the 128x512x1024 precision-study grid
 @pytest.mark.parametrize("conj", [0, 1])
 def test_conv3d_matches_oracle(cdx, oracle, torch_cuda, tmp_path, shape, conj):
