@@ -13,8 +13,9 @@ cdx_RL_batch_device (one CUDA graph of every stack's iterations).
             launch stream; voxel-iterations/s of all decon grids
   forms   : the same in the mixed-precision form (x-pass DFT stages as
             tcgen05 MMAs in split TF32) and the ratio mixed / plain
-  e2e     : the same call with host buffers: each step copies the 64 raw
-            stacks in from pinned host memory and the 64 results out
+  e2e     : the same batch with host buffers (cdx_RL_batch_host): each
+            step uploads the 64 raw stacks from pinned host memory and
+            downloads the 64 results, inside the call's graph
   roofline: 56 B of algorithmic traffic per voxel-iteration over the
             measured HBM copy bandwidth, for the batch step; the per-pass
             roofline of one iteration is in secondary.stage_scan
@@ -411,26 +412,19 @@ def measure_batch(cdx, torch, dev, stream, stacks, steps, warmup, form):
     return ms, vox * iters, launches, finite
 
 
-def measure_batch_e2e(cdx, torch, dev, stream, stacks, reps):
-    """The batch with host buffers: pinned u16 stacks copied in, results out,
-    inside the timed region (wall clock)."""
+def measure_batch_e2e(cdx, torch, stacks, reps):
+    """The batch with host buffers, through cdx_RL_batch_host: the 64 raw
+    stacks in pinned host memory are uploaded and the results downloaded by
+    the call itself (each stack's transfers are nodes of its chain in the
+    graph, overlapping other stacks' iterations); wall clock per call."""
     iters = BATCH["iterations"]
-    h_raw = [d["raw"].cpu().pin_memory() for d in stacks]
-    dev_stacks = [dict(d) for d in stacks]
-    outs = cdx.rl_batch(dev_stacks, n_iters=iters, stream=stream)
-    h_out = [torch.empty(o.shape, dtype=torch.float32).pin_memory() for o in outs]
-    stream.synchronize()
+    host = [dict(d, raw=d["raw"].cpu().pin_memory()) for d in stacks]
+    outs = cdx.rl_batch_host(host, n_iters=iters)
     t0 = time.perf_counter()
     for _ in range(reps):
-        with torch.cuda.stream(stream):
-            for d, h in zip(dev_stacks, h_raw):
-                d["raw"].copy_(h, non_blocking=True)
-            outs = cdx.rl_batch(dev_stacks, n_iters=iters, stream=stream)
-            for o, h in zip(outs, h_out):
-                h.copy_(o, non_blocking=True)
-        stream.synchronize()
+        outs = cdx.rl_batch_host(host, n_iters=iters, results=outs)
     s = (time.perf_counter() - t0) / reps
-    return s, int(sum(h.numel() * 2 for h in h_raw)), int(sum(h.numel() * 4 for h in h_out))
+    return s, int(sum(h["raw"].numel() * 2 for h in host)), int(sum(o.numel() * 4 for o in outs))
 
 
 def measure_stage_scan(cdx, torch, dev, steps, pg):
@@ -722,8 +716,7 @@ def run_gb300(args):
     ms_mixed = max_over_ranks(ms_mixed, pg, dev)
     value_mixed = world * vox_iters / (ms_mixed * 1e-3)
     # ---- e2e (host buffers)
-    e2e_s, h2d, d2h = measure_batch_e2e(cdx, torch, dev, stream, stacks,
-                                        max(1, min(args.steps, 5)))
+    e2e_s, h2d, d2h = measure_batch_e2e(cdx, torch, stacks, max(1, min(args.steps, 5)))
     e2e_s = max_over_ranks(e2e_s, pg, dev)
     L.cdx_batch_release()
     del stacks
@@ -760,7 +753,7 @@ def run_gb300(args):
                       "mixed_over_plain": value_mixed / value},
             "e2e": {"value": world * vox_iters / e2e_s, "unit": "voxel-iter/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "host_buffers": "pinned"},
+                    "host_buffers": "pinned", "api": "cdx_RL_batch_host"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None,
                          "nominal_gbs": NOMINAL_HBM_GBS,

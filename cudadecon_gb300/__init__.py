@@ -134,6 +134,7 @@ def _bind(L) -> None:
         "cdx_batch_grid": (c_int, [c_int, c_int, c_int, POINTER(c_int), POINTER(c_int),
                                    POINTER(c_int)]),
         "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
+        "cdx_RL_batch_host": (c_int, [POINTER(BatchStack), c_int, c_int]),
         "cdx_batch_last_launch_count": (c_longlong, []),
         "cdx_batch_release": (None, []),
     }
@@ -366,6 +367,34 @@ def rl_batch(stacks, n_iters=10, stream=None):
     ok = L.cdx_RL_batch_device(arr, n, int(n_iters), c_void_p(stream.cuda_stream))
     if ok != 1:
         _err("cdx_RL_batch_device")
+    return outs
+
+
+def rl_batch_host(stacks, n_iters=10, results=None):
+    """cdx_RL_batch_host: like rl_batch, but `raw` of each stack is a
+    page-locked (pinned) CPU uint16 tensor and the results are written into
+    pinned CPU float32 tensors (allocated here unless `results` gives them).
+    Returns the results once they are complete."""
+    import torch
+    L = lib()
+    n = len(stacks)
+    arr = (BatchStack * n)()
+    keep, outs = [], []
+    for i, d in enumerate(stacks):
+        raw = d["raw"]
+        nz, ny, nx = raw.shape
+        gz, gy, gx = batch_grid((nz, ny, nx))
+        out = results[i] if results is not None else \
+            torch.empty((gz, gy, gx), dtype=torch.float32).pin_memory()
+        img = np.ascontiguousarray(synth.otf_table_to_image(d["otf"]), dtype=np.float32)
+        keep.append(img)
+        outs.append(out)
+        arr[i] = BatchStack(raw.data_ptr(), nx, ny, nz, out.data_ptr(), _fptr(img), img.shape[1],
+                            img.shape[0], d.get("dr", 0.104), d.get("dz", 0.3),
+                            d.get("dr_psf", 0.104), d.get("dz_psf", 0.1),
+                            d.get("background", 100.0))
+    if L.cdx_RL_batch_host(arr, n, int(n_iters)) != 1:
+        _err("cdx_RL_batch_host")
     return outs
 
 

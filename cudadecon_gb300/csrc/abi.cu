@@ -724,9 +724,18 @@ struct BatchStack {
   DevBuf<double> partials;
   DevBuf<float> lam;
   float* final_x = nullptr;
+  // host mode (cdx_RL_batch_host): the stack's device copy of the caller's
+  // page-locked raw buffer, and what the captured graph baked in
+  DevBuf<unsigned short> u16;
+  const unsigned short* h_raw = nullptr;
+  float* h_result = nullptr;
+  float background = 0.f;
   void release() {
     plan.release();
     raw_otf.release();
+    u16.release();
+    h_raw = nullptr;
+    h_result = nullptr;
     Xa.release();
     Xb.release();
     G.release();
@@ -746,6 +755,7 @@ struct Batch {
   cudaGraphExec_t exec = nullptr;
   int graph_iters = -1;
   int graph_form = -1;  // DFT form the graph's kernels were captured with
+  int graph_host = -1;  // 1 when the graph carries the host transfers
   long long graph_launches = 0;
   long long last_launches = 0;
   void drop_graph() {
@@ -753,6 +763,7 @@ struct Batch {
     exec = nullptr;
     graph_iters = -1;
     graph_form = -1;
+    graph_host = -1;
   }
   void release() {
     drop_graph();
@@ -837,8 +848,10 @@ static int batch_setup_stack(BatchStack& b, const cdx_batch_stack& d, bool* chan
   return 0;
 }
 
-// Capture the iterations of every stack into b.exec.
-static int batch_capture(Batch& b, int nIters) {
+// Capture the iterations of every stack into b.exec; with host, each
+// stack's chain also uploads and conditions its raw stack first and
+// downloads its result last.
+static int batch_capture(Batch& b, int nIters, bool host) {
   b.drop_graph();
   std::vector<int> order(b.st.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
@@ -860,6 +873,20 @@ static int batch_capture(Batch& b, int nIters) {
     BatchStack& t = b.st[order[j]];
     cudaStream_t s = b.fan[j % K];
     const size_t n = (size_t)t.gx * t.gy * t.gz;
+    if (host) {
+      // the stack's upload and conditioning head its chain
+      const size_t nin = (size_t)t.nx * t.ny * t.nz;
+      if ((e = cudaMemcpyAsync(t.u16.p, t.h_raw, nin * sizeof(unsigned short),
+                               cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+        set_cuda_error("batch capture", e);
+        rc = e;
+        break;
+      }
+      if ((rc = launch_u16_to_f32_crop(t.u16.p, t.nx, t.ny, t.gx, t.gy, t.gz, t.Xa.p,
+                                       t.background, 1, s)))
+        break;
+      ++launches;
+    }
     if ((e = cudaMemsetAsync(t.lam.p, 0, 2 * sizeof(float), s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(t.raw.p, t.Xa.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s)) !=
             cudaSuccess) {
@@ -870,6 +897,15 @@ static int batch_capture(Batch& b, int nIters) {
     const LoopBufs lb{t.Xa.p, t.Xb.p, t.G.p, t.raw.p, t.S.p, t.partials.p, t.lam.p,
                       (int)(t.partials.n / 2)};
     rc = rl_loop(t.plan, lb, nIters, s, false, &t.final_x, &launches);
+    if (!rc && host) {
+      // and its download ends it (nIters == 0: the conditioned stack)
+      const float* src = nIters > 0 ? t.final_x : t.Xa.p;
+      if ((e = cudaMemcpyAsync(t.h_result, src, n * sizeof(float), cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess) {
+        set_cuda_error("batch capture", e);
+        rc = e;
+      }
+    }
   }
   for (int k = 0; k < K && !rc; ++k) {
     if ((e = cudaEventRecord(b.ev_join[k], b.fan[k])) != cudaSuccess ||
@@ -899,11 +935,14 @@ static int batch_capture(Batch& b, int nIters) {
   }
   b.graph_iters = nIters;
   b.graph_form = dft_form();
+  b.graph_host = host ? 1 : 0;
   b.graph_launches = launches;
   return 0;
 }
 
-static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStream_t caller) {
+// host: raw and result are page-locked host buffers (cdx_RL_batch_host).
+static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStream_t caller,
+                     bool host) {
   Batch& b = g_b;
   if (!stacks || n < 1 || nIters < 0) {
     set_error("cdx_RL_batch_device", "need at least one stack and nIters >= 0");
@@ -947,8 +986,22 @@ static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStrea
     changed = changed || c;
   }
   if (changed) b.drop_graph();
-  // after the caller's queued work: the OTF tables, then the cropped,
-  // background-subtracted stacks (into each stack's first estimate)
+  if (host) {
+    // the graph bakes in the host buffers and backgrounds
+    for (int i = 0; i < n; ++i) {
+      BatchStack& t = b.st[i];
+      const cdx_batch_stack& d = stacks[i];
+      if ((rc = t.u16.ensure((size_t)d.nx * d.ny * d.nz))) return rc;
+      if (t.h_raw != d.raw || t.h_result != d.result || t.background != d.background)
+        b.drop_graph();
+      t.h_raw = d.raw;
+      t.h_result = d.result;
+      t.background = d.background;
+    }
+  }
+  // after the caller's queued work: the OTF tables, then (device buffers)
+  // the cropped, background-subtracted stacks (into each stack's first
+  // estimate)
   CDX_CHECK(cudaEventRecord(b.ev_in, caller));
   CDX_CHECK(cudaStreamWaitEvent(b.origin, b.ev_in, 0));
   long long launches = 0;
@@ -962,19 +1015,28 @@ static int batch_run(const cdx_batch_stack* stacks, int n, int nIters, cudaStrea
     } else {
       if ((rc = fill_otf(t.plan, t.dr, t.dz, t.os, b.origin))) return rc;
     }
+    launches += 1;
+    if (host) continue;
     if ((rc = launch_u16_to_f32_crop(d.raw, d.nx, d.ny, t.gx, t.gy, t.gz, t.Xa.p, d.background, 1,
                                      b.origin)))
       return rc;
-    launches += 2;
+    launches += 1;
   }
-  if (nIters > 0) {
-    if (!b.exec || b.graph_iters != nIters || b.graph_form != dft_form()) {
+  if (nIters > 0 || host) {
+    if (!b.exec || b.graph_iters != nIters || b.graph_form != dft_form() ||
+        b.graph_host != (host ? 1 : 0)) {
       // the plans' tables were built on the origin stream
       CDX_CHECK(cudaStreamSynchronize(b.origin));
-      if ((rc = batch_capture(b, nIters))) return rc;
+      if ((rc = batch_capture(b, nIters, host))) return rc;
     }
     CDX_CHECK(cudaGraphLaunch(b.exec, b.origin));
     launches += b.graph_launches;
+  }
+  if (host) {
+    // the results are in the caller's host buffers when this returns
+    CDX_CHECK(cudaStreamSynchronize(b.origin));
+    b.last_launches = launches;
+    return 0;
   }
   for (int i = 0; i < n; ++i) {
     BatchStack& t = b.st[i];
@@ -1450,7 +1512,30 @@ int cdx_batch_grid(int nx, int ny, int nz, int* gx, int* gy, int* gz) {
 
 int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
-  return batch_run(stacks, n, nIters, (cudaStream_t)stream) == 0 ? 1 : 0;
+  return batch_run(stacks, n, nIters, (cudaStream_t)stream, false) == 0 ? 1 : 0;
+}
+
+int cdx_RL_batch_host(const cdx_batch_stack* stacks, int n, int nIters) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!stacks || n < 1) {
+    set_error("cdx_RL_batch_host", "need at least one stack and nIters >= 0");
+    return 0;
+  }
+  for (int i = 0; i < n; ++i) {
+    const void* ptrs[2] = {stacks[i].raw, stacks[i].result};
+    for (const void* ptr : ptrs) {
+      cudaPointerAttributes at;
+      if (!ptr || cudaPointerGetAttributes(&at, ptr) != cudaSuccess ||
+          at.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        set_error("cdx_RL_batch_host",
+                  "raw and result must be page-locked host buffers (cudaHostAlloc or "
+                  "cudaHostRegister); use RL_interface or cdx_RL_batch_device otherwise");
+        return 0;
+      }
+    }
+  }
+  return batch_run(stacks, n, nIters, nullptr, true) == 0 ? 1 : 0;
 }
 
 long long cdx_batch_last_launch_count(void) { return g_b.last_launches; }

@@ -307,6 +307,15 @@ int cdx_batch_grid(int nx, int ny, int nz, int* gx, int* gy, int* gz);
  * (cdx_last_error()). */
 int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* stream);
 
+/* cdx_RL_batch_device with the stacks and results in host memory: raw and
+ * result of every stack are page-locked host buffers (cudaHostAlloc or
+ * cudaHostRegister; pageable memory is rejected).  Each stack's upload,
+ * conditioning and download are nodes of its chain in the captured graph,
+ * so transfers overlap the other stacks' iterations; the graph is also kept
+ * while the host buffers and backgrounds stay the same.  Returns 1 once the
+ * results are in the host buffers, 0 on failure (extension). */
+int cdx_RL_batch_host(const cdx_batch_stack* stacks, int n, int nIters);
+
 /* Number of kernel launches (graph nodes included) of the last batch call. */
 long long cdx_batch_last_launch_count(void);
 

@@ -89,3 +89,34 @@ def test_batch_zero_iterations_returns_conditioned_stack(cdx, torch_cuda, tmp_pa
         want = np.maximum(d["raw_np"][:gz, :gy, :gx].astype(np.float32) - d["background"], 0)
         assert np.array_equal(o.cpu().numpy(), want)
     cdx.lib().cdx_batch_release()
+
+
+def test_batch_host_buffers_match_device_batch(cdx, torch_cuda):
+    """cdx_RL_batch_host (pinned host stacks and results, transfers inside
+    the graph) gives the device batch's results bit for bit, on repeated
+    calls, after new host buffers (the graph is captured again), and for
+    nIters = 0 (the conditioned stacks)."""
+    torch = torch_cuda
+    st = _stacks(torch)
+    ref = [o.cpu().numpy() for o in cdx.rl_batch(st, n_iters=5)]
+    torch.cuda.synchronize()
+    host = [dict(d, raw=d["raw"].cpu().pin_memory()) for d in st]
+    for _ in range(2):
+        outs = cdx.rl_batch_host(host, n_iters=5)
+        for o, r in zip(outs, ref):
+            assert np.array_equal(o.numpy(), r)
+    host2 = [dict(d, raw=d["raw"].clone().pin_memory()) for d in host]
+    for o, r in zip(cdx.rl_batch_host(host2, n_iters=5), ref):
+        assert np.array_equal(o.numpy(), r)
+    for d, o in zip(st, cdx.rl_batch_host(host2, n_iters=0)):
+        gz, gy, gx = cdx.batch_grid(d["raw_np"].shape)
+        want = np.maximum(d["raw_np"][:gz, :gy, :gx].astype(np.float32) - d["background"], 0)
+        assert np.array_equal(o.numpy(), want)
+    cdx.lib().cdx_batch_release()
+
+
+def test_batch_host_rejects_pageable_buffers(cdx, torch_cuda):
+    st = _stacks(torch_cuda)[:1]
+    host = [dict(st[0], raw=st[0]["raw"].cpu())]  # not pinned
+    with pytest.raises(cdx.CudaDeconError, match="page-locked"):
+        cdx.rl_batch_host(host, n_iters=2)
