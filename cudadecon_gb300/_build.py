@@ -24,6 +24,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str
 SOURCES = ["decon_kernels.cu", "decon_x_fwd.cu", "decon_x_ratio.cu", "decon_x_update.cu", "decon_x_tc.cu", "decon_y.cu", "decon_z.cu", "geometry.cu", "affine.cu", "accel.cu", "accel_noalloc.cu", "abi.cu", "otf_make.cu", "wiener.cu", "tiles.cu", "otf_io.cpp"]
 
 
+# the generated units of the x-pass plans (gen_plans.py)
+SOURCES += sorted(p.name for p in CSRC.glob("decon_x_gen_*.cu"))
+
+
 def nvcc() -> str:
     cand = os.environ.get("NVCC") or "/usr/local/cuda/bin/nvcc"
     return cand if Path(cand).exists() else "nvcc"

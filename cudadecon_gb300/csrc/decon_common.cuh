@@ -155,13 +155,14 @@ static inline size_t fft_smem(int L, long long tile, long long extra = 0) {
   return sizeof(float2) * ((size_t)L + spad_size((int)tile) + (size_t)extra);
 }
 
-// Allow a kernel the dynamic shared memory it is launched with (the default
-// limit is 48 KB; long rows need more).
+// Allow a kernel the dynamic shared memory it is launched with.  The default
+// limit is 48 KB for static and dynamic shared memory together, so the
+// attribute is raised for every launch, not only past 48 KB of dynamic
+// memory (a kernel with static shared memory crosses the limit earlier).
 template <class K>
 static int smem_optin(K kernel, size_t bytes) {
   // prefer the largest shared-memory carveout so that several tiles fit an SM
   CDX_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-  if (bytes <= 48 * 1024) return 0;
   CDX_CHECK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return 0;
 }

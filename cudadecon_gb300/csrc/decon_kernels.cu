@@ -106,6 +106,10 @@ int fft_len_init(FftLen& f, int L) {
   if (f.has_xr) {
     if (int rc = build_fft_dev(L, rad, f.xrdev, &f.d_twxr)) return rc;
   }
+  f.has_gx = gx_radices(L, rad);
+  if (f.has_gx) {
+    if (int rc = build_fft_dev(L, rad, f.gxdev, &f.d_twgx)) return rc;
+  }
   int q0 = 0, q1 = 0;
   f.has_tc = tc_plan_radices(L, q0, q1);
   if (f.has_tc) {
@@ -135,6 +139,10 @@ void fft_len_free(FftLen& f) {
   if (f.d_tw) cudaFree(f.d_tw);
   if (f.d_tws) cudaFree(f.d_tws);
   if (f.d_twxr) cudaFree(f.d_twxr);
+  if (f.d_twgx) cudaFree(f.d_twgx);
+  f.d_twgx = nullptr;
+  f.gxdev.tw = nullptr;
+  f.has_gx = false;
   f.d_tw = nullptr;
   f.d_tws = nullptr;
   f.d_twxr = nullptr;

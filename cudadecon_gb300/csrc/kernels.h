@@ -72,6 +72,10 @@ struct FftLen {
   bool has_xr = false;
   FftDev xrdev;
   float2* d_twxr = nullptr;
+  // the generated x-pass plan of the length, if it has one
+  bool has_gx = false;
+  FftDev gxdev;
+  float2* d_twgx = nullptr;
   // the tensor-core plan of the length, if it has one
   bool has_tc = false;
   TcTables tc;

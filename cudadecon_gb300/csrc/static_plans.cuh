@@ -44,6 +44,10 @@ namespace cdx {
 CDX_SPLAN_LIST(CDX_DEF_SPLAN)
 #undef CDX_DEF_SPLAN
 
+#define CDX_DEF_GXPLAN(L, ...) using SPX##L = SPlan<L, __VA_ARGS__>;
+CDX_GEN_X_SPLANS(CDX_DEF_GXPLAN)
+#undef CDX_DEF_GXPLAN
+
 #define CDX_DEF_XRPLAN(L, P, ...) using SPR##L = SPlan<L, __VA_ARGS__>;
 CDX_XR_PLANS(CDX_DEF_XRPLAN)
 #undef CDX_DEF_XRPLAN
@@ -66,6 +70,20 @@ inline bool static_radices(int L, std::vector<int>& rad) {
     return true;
     CDX_SPLAN_LIST(CDX_RAD_CASE)
 #undef CDX_RAD_CASE
+    default:
+      return false;
+  }
+}
+
+// Radices of the generated x-pass plan for length L (false when it has none).
+inline bool gx_radices(int L, std::vector<int>& rad) {
+  switch (L) {
+#define CDX_GX_CASE(LL, ...) \
+  case LL:                   \
+    rad = {__VA_ARGS__};     \
+    return true;
+    CDX_GEN_X_SPLANS(CDX_GX_CASE)
+#undef CDX_GX_CASE
     default:
       return false;
   }

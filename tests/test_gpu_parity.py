@@ -58,7 +58,9 @@ def _oracle_state(oracle, shape_zyx, table, **kw):
                                    # generated compile-time plans (y in [128, 512], z in
                                    # [32, 160]): two radices, three (343 = 7*7*7), odd
                                    (35, 135, 40), (49, 343, 24), (125, 500, 30),
-                                   (147, 160, 20), (45, 405, 36)])
+                                   (147, 160, 20), (45, 405, 36),
+                                   # generated x-pass plans (x in [128, 1024])
+                                   (6, 10, 135), (5, 7, 343), (4, 9, 1000), (3, 12, 882)])
 def test_rfft3d_matches_numpy(cdx, torch_cuda, shape):
     torch = torch_cuda
     nz, ny, nx = shape

@@ -302,3 +302,27 @@ def test_camcor_then_rl_chain_vs_reference_camcor_and_oracle(cdx, oracle, ref, t
     print(f"\ncamcor -> deskew -> 20 it -> rotate on {shape}: rel L2 vs oracle {e:.2e}")
     assert mine.shape == want.shape
     assert e < 1e-5
+
+
+@pytest.mark.parametrize("shape", [(12, 20, 243), (10, 16, 245), (8, 24, 1000), (9, 30, 135)])
+def test_rl_generated_x_plans_vs_reference(cdx, oracle, ref, torch_cuda, tmp_path, shape):
+    """RL through the generated compile-time x plans (x in [128, 1024] outside
+    the hand-tuned registry; 243 and 245 need just over 48 KB of shared
+    memory in the update pass) against the reference's kernels + cuFFT."""
+    raw = synth.bead_stack(shape, n_beads=40, psf_sigma_xy=1.3, psf_sigma_z=2.5, seed=sum(shape))
+    nz, ny, nx = shape
+    tab = synth.gaussian_otf_table(129, 64, 1.3, 2.5)
+    p = tmp_path / "otf.tif"
+    synth.write_otf(p, tab)
+    kw = dict(dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.25)
+    cdx.rl_init(shape, p, **kw)
+    gz, gy, gx = cdx.decon_grid()
+    mine = cdx.rl_decon(raw, background=100.0, n_iters=8)
+    cdx.rl_cleanup()
+    st = oracle.rl_init(nx, ny, nz, kw["dr"], kw["dz"], kw["dr_psf"], kw["dz_psf"], 0.0, 0.0, 0,
+                        False, synth.otf_table_to_image(tab))
+    X0 = oracle.bgsub(raw[:gz, :gy, :gx].astype(np.float32), 100.0)
+    theirs, _ = ref.rl_iterations(X0, X0, tab, oracle.kscales(st, gx, gy, gz), 8)
+    e = rel_l2(mine, theirs)
+    print(f"\ngenerated x plan {gz}x{gy}x{gx}, 8 it: rel L2 vs reference {e:.2e}")
+    assert e < 1e-5
