@@ -3,6 +3,9 @@
 * geom_oracle.c -> oracle/_build/libgeom_oracle.so, with -ffp-contract=off (so
   the compiler adds no fused multiply-adds beyond the explicit fma() calls;
   gcc on aarch64 would otherwise contract).
+* The reference's makeOTF (src/radialft_interface.cpp) with stand-ins for
+  FFTW and libtiff (oracle/shim/) into oracle/_ref/libradialft_ref.so, only
+  where the reference is present (it generates the OTF fixtures).
 * The reference's own CUDA kernels, compiled from its sources where they lie
   (src/{RLgpuImpl,geometryTransform,camcor}.cu of the reference checkout, with
   its Buffers/ headers) to PTX in oracle/_ref/ — only where the reference is
@@ -77,8 +80,38 @@ def build_ref_runner() -> Path | None:
     return out
 
 
+SHIM = HERE / "shim"
+
+
+def build_radialft_ref() -> Path | None:
+    """The reference's makeOTF (src/radialft_interface.cpp, compiled where it
+    lies) with the FFTW and libtiff stand-ins of oracle/shim/, into
+    oracle/_ref/libradialft_ref.so; only where the reference is present."""
+    src = REF_SRC / "radialft_interface.cpp"
+    if not src.exists():
+        return None
+    REF_OUT.mkdir(exist_ok=True)
+    out = REF_OUT / "libradialft_ref.so"
+    deps = [src, SHIM / "fftw_shim.cpp", SHIM / "tiff_capture.cpp", SHIM / "fftw3.h",
+            SHIM / "tiffio.h"]
+    if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return out
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Dcimg_display=0", f"-I{SHIM}",
+           f"-I{REF_SRC}", str(src), str(SHIM / "fftw_shim.cpp"), str(SHIM / "tiff_capture.cpp"),
+           "-o", str(out), "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print("reference makeOTF not built:", r.stderr[-2000:])
+        return None
+    return out
+
+
 def build_all() -> None:
     build_geom()
+    try:
+        build_radialft_ref()
+    except (subprocess.CalledProcessError, OSError) as e:
+        print("reference makeOTF not built:", e)
     try:
         if build_ref_ptx():
             build_ref_runner()

@@ -10,9 +10,14 @@ double evaluation written out (np.float32 for `float`, Python floats for
 `double`).  The FFT is numpy's (float64); the reference calls FFTW in float
 (absent here), so results agree to FFT rounding, not bit for bit.
 
-Parity status: pinned to the reference's arithmetic by restatement only (no
-golden OTF ships with the reference); the tests check the restatement
-against analytic OTFs of Gaussian beads.
+Parity status: pinned.  No golden OTF ships with the reference, so its own
+makeOTF was run here (src/radialft_interface.cpp compiled from its source
+with stand-ins for FFTW and libtiff, oracle/radialft_ref.py) on seeded PSFs
+with the argument sets the tests use; its outputs are the fixtures in
+tests/golden/golden_otf.npz (tests/golden/make_otf_golden.py), and this
+restatement agrees with them to relative L2 below 1e-6
+(tests/test_otf_cpu.py).  The tests also check it against analytic OTFs of
+Gaussian beads.
 """
 
 from __future__ import annotations

@@ -68,3 +68,24 @@ def test_make_otf_rejects_unsupported_sizes(cdx, torch_cuda):
     psf = _psf(shape=(11, 64, 64), center=(5.0, 32.0, 32.0))
     with pytest.raises(cdx.CudaDeconError):
         cdx.make_otf(psf)
+
+
+@pytest.mark.parametrize("case", ["default", "interpkr6", "user_background", "cleanup", "wide",
+                                  "out_3d"])
+def test_make_otf_matches_reference_makeotf_fixtures(cdx, torch_cuda, case):
+    """cdx_make_otf against the reference's own makeOTF output
+    (tests/golden/golden_otf.npz, tests/golden/make_otf_golden.py)."""
+    from pathlib import Path
+    from golden.make_otf_golden import CASES, psf
+    name, shape, center, sxy, sz, seed, kw = next(c for c in CASES if c[0] == case)
+    want = np.load(Path(__file__).resolve().parent / "golden" / "golden_otf.npz")[name]
+    p = psf(shape, center, sxy, sz, seed)
+    args = {k: v for k, v in dict(dr=kw.get("dr"), dz=kw.get("dz"), lambdanm=kw.get("lambdanm"),
+                                  interpkr=kw.get("interpkr"), background=kw.get("user_background"),
+                                  NA=kw.get("NA"), cleanup=kw.get("do_cleanup")).items()
+            if v is not None}
+    if kw.get("out_3d"):
+        args["otf_3d"] = True
+    got = cdx.make_otf(p, **args).view(np.complex64)
+    assert got.shape == want.shape
+    assert rel_l2(got, want) < TOL

@@ -4,10 +4,14 @@ the library's TIFF writer read back by its TIFF reader (no GPU needed)."""
 
 import math
 
+from pathlib import Path
+
 import numpy as np
 import pytest
 
 from oracle import otf_oracle as OO
+
+ROOT_GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def gaussian_bead(shape, center, sxy, sz, amp=1000.0, bg=100.0):
@@ -74,3 +78,29 @@ def test_float_tiff_writer_roundtrip(cdx, tmp_path):
 def test_make_otf_missing_file_returns_one(cdx, tmp_path):
     assert cdx.lib().makeOTF(str(tmp_path / "nope.tif").encode(), str(tmp_path / "o.tif").encode(),
                              520, 0.1, 10, False, 90.0, 1.25, 1.3, 0.1, 0, False, False) == 1
+
+
+def _golden_otf_cases():
+    from golden.make_otf_golden import CASES
+    return CASES
+
+
+@pytest.mark.parametrize("case", [c[0] for c in _golden_otf_cases()])
+def test_otf_oracle_matches_reference_makeotf_fixtures(case):
+    """The oracle's restatement of makeOTF against the reference's own
+    makeOTF (its source compiled with stand-ins for FFTW and libtiff;
+    tests/golden/make_otf_golden.py)."""
+    from conftest import rel_l2
+    from golden.make_otf_golden import CASES, psf
+    name, shape, center, sxy, sz, seed, kw = next(c for c in CASES if c[0] == case)
+    want = np.load(ROOT_GOLDEN / "golden_otf.npz")[name]
+    p = psf(shape, center, sxy, sz, seed)
+    if kw.get("out_3d"):
+        got = OO.make_otf_3d(p)
+    else:
+        got = OO.make_otf(p, dr=kw.get("dr", 0.102), dz=kw.get("dz", 0.102),
+                          lambdanm=kw.get("lambdanm", 520), interpkr=kw.get("interpkr", 10),
+                          user_background=kw.get("user_background"), NA=kw.get("NA", 1.25),
+                          do_cleanup=kw.get("do_cleanup", False))
+    assert got.shape == want.shape
+    assert rel_l2(got, want) < 1e-6
