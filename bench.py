@@ -668,6 +668,60 @@ def measure_batch_per_stack(cdx, torch, dev, stacks):
             "unit": "voxel-iter/s", "seconds": s}
 
 
+def measure_one_stack(cdx, torch, dev, zyx, steps, warmup):
+    """One synthetic stack of shape zyx (u16 beads on a Poisson background,
+    the batch's Gaussian OTF), 10 RL iterations per cdx_RL_device call:
+    voxel-iter/s and the per-pass times of one iteration (for profiling and
+    for tuning one length's plans)."""
+    from cudadecon_gb300 import synth
+    L = cdx.lib()
+    nz, ny, nx = zyx
+    iters = BATCH["iterations"]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(nz * 1000003 + ny * 1009 + nx)
+    lam = 100.0 + 3000.0 * (torch.rand(zyx, generator=gen, device=dev) < 2e-4).float()
+    raw = torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.uint16)
+    td = tempfile.TemporaryDirectory()
+    p = Path(td.name) / "otf.tif"
+    synth.write_otf(p, synth.gaussian_otf_table(129, 64, 1.5, 4.0))
+    cdx.rl_init(zyx, p, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.3)
+    gz, gy, gx = cdx.decon_grid()
+    out = torch.empty(cdx.output_shape(), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        if L.cdx_RL_device(ctypes.c_void_p(raw.data_ptr()), nx, ny, nz,
+                           ctypes.c_void_p(out.data_ptr()), None, 100.0, False, False, iters,
+                           0, 0, 0, 0.0, False, False, sp) != 1:
+            raise RuntimeError(L.cdx_last_error().decode())
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            step()
+    stream.synchronize()
+    ms = events_ms(torch, stream, step, steps)
+    L.cdx_profile_enable(1)
+    with torch.cuda.stream(stream):
+        step()
+    stream.synchronize()
+    pm = (ctypes.c_double * 9)()
+    pn = (ctypes.c_longlong * 9)()
+    it_ms = ctypes.c_double(0)
+    it_n = ctypes.c_longlong(0)
+    L.cdx_profile_read(pm, pn, 9, ctypes.byref(it_ms), ctypes.byref(it_n))
+    L.cdx_profile_enable(0)
+    passes = {L.cdx_profile_pass_name(i).decode(): round(pm[i] / max(pn[i], 1), 5)
+              for i in range(9)}
+    vox = gz * gy * gx
+    cdx.rl_cleanup()
+    td.cleanup()
+    return {"workload": f"one stack {nz}x{ny}x{nx} u16, {iters} RL it",
+            "decon_grid_zyx": [gz, gy, gx], "value": vox * iters / (ms * 1e-3),
+            "unit": "voxel-iter/s", "ms_per_step": ms, "pass_ms": passes,
+            "output_finite": bool(torch.isfinite(out).all().item())}
+
+
 def run_only(args):
     """One workload alone (for profiling): prints its JSON result."""
     import torch
@@ -680,6 +734,9 @@ def run_only(args):
         r = measure_grid3(cdx, torch, dev, args.steps)
     elif args.only == "timelapse":
         r = measure_timelapse(cdx, torch, dev, args.steps)
+    elif args.only == "stack":
+        zyx = tuple(int(v) for v in args.zyx.split(","))
+        r = measure_one_stack(cdx, torch, dev, zyx, args.steps, args.warmup)
     else:
         r = measure_batch_per_stack(cdx, torch, dev, batch_inputs(dev))
     print(json.dumps({"only": args.only, **r}), flush=True)
@@ -783,8 +840,11 @@ def main():
                     help="only the batched headline workload")
     ap.add_argument("--no-timelapse", action="store_true",
                     help="skip the 16-stack time-lapse secondary workload")
-    ap.add_argument("--only", choices=["stage_scan", "grid3", "timelapse", "batch_per_stack"],
+    ap.add_argument("--only", choices=["stage_scan", "grid3", "timelapse", "batch_per_stack",
+                                       "stack"],
                     help="run one workload alone and print its result (for profiling)")
+    ap.add_argument("--zyx", default="100,256,600",
+                    help="stack shape z,y,x of --only stack")
     args = ap.parse_args()
     if args.only:
         return run_only(args)

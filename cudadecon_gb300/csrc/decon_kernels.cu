@@ -110,6 +110,10 @@ int fft_len_init(FftLen& f, int L) {
   if (f.has_gx) {
     if (int rc = build_fft_dev(L, rad, f.gxdev, &f.d_twgx)) return rc;
   }
+  f.has_gz = gz_radices(L, rad);
+  if (f.has_gz) {
+    if (int rc = build_fft_dev(L, rad, f.gzdev, &f.d_twgz)) return rc;
+  }
   int q0 = 0, q1 = 0;
   f.has_tc = tc_plan_radices(L, q0, q1);
   if (f.has_tc) {
@@ -143,6 +147,10 @@ void fft_len_free(FftLen& f) {
   f.d_twgx = nullptr;
   f.gxdev.tw = nullptr;
   f.has_gx = false;
+  if (f.d_twgz) cudaFree(f.d_twgz);
+  f.d_twgz = nullptr;
+  f.gzdev.tw = nullptr;
+  f.has_gz = false;
   f.d_tw = nullptr;
   f.d_tws = nullptr;
   f.d_twxr = nullptr;
@@ -176,6 +184,8 @@ int x_pass_blocks(const Geom& g) {
   std::vector<int> rad;
   int pxr = 0;
   if (xr_radices(g.nx, rad, pxr) && pxr < p) p = pxr;
+  int pgx = 0;
+  if (gx_pairs(g.nx, pgx) && pgx < p) p = pgx;
   return ceil_div(g.ny, 2 * p) * g.nz;
 }
 

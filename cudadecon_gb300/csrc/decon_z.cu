@@ -222,16 +222,16 @@ int launch_z_pass(const Geom& g, const FftLen& fz, float2* S, const OtfDev& otf,
                                                        splan_threads<SP##L, WW>(), st);
       CDX_Z_PLANS(CDX_CASE)
 #undef CDX_CASE
-#define CDX_GCASE(L, WW)                                                                       \
-  case L:                                                                                      \
-    if (otf.mode == 0)                                                                         \
-      return conj ? z_go<StaticRunner<SP##L, WW, true>, 0, 1>(g, fz.sdev, S, otf, conj,        \
-                                                             fwd_only, WW,                     \
-                                                             splan_threads<SP##L, WW>(), st)   \
-                  : z_go<StaticRunner<SP##L, WW, true>, 0, 0>(g, fz.sdev, S, otf, conj,        \
-                                                             fwd_only, WW,                     \
-                                                             splan_threads<SP##L, WW>(), st);  \
-    break;
+      default:
+        break;
+    }
+  if (fz.has_gz && otf.mode == 0) switch (g.nz) {
+#define CDX_GCASE(L, WW, RR)                                                                  \
+  case L:                                                                                     \
+    return conj ? z_go<StaticRunner<SPZ##L, WW, true, false, RR>, 0, 1>(                      \
+                      g, fz.gzdev, S, otf, conj, fwd_only, WW, splan_threads<SPZ##L, WW>(), st) \
+                : z_go<StaticRunner<SPZ##L, WW, true, false, RR>, 0, 0>(                      \
+                      g, fz.gzdev, S, otf, conj, fwd_only, WW, splan_threads<SPZ##L, WW>(), st);
       CDX_Z_GEN_PLANS(CDX_GCASE)
 #undef CDX_GCASE
       default:

@@ -286,18 +286,20 @@ struct GenericRunner {
 
 // GTW: the stage twiddles are read from the global table (through the
 // read-only cache) instead of a shared-memory copy, which saves the kernel
-// L float2s of shared memory.
-template <class Plan, int V, bool VFAST, bool GTW = false>
+// L float2s of shared memory.  REGX: registers per thread added to the
+// estimate behind the launch bounds (fewer blocks per SM, more registers
+// for each thread).
+template <class Plan, int V, bool VFAST, bool GTW = false, int REGX = 0>
 struct StaticRunner {
   static constexpr bool kStatic = true;
   static constexpr int kV = V;
   static constexpr int kThreads = splan_threads<Plan, V>();
   // Blocks per SM to ask the compiler to fit (launch bounds): TARGET, lowered
-  // so that each thread keeps about 2*qmax + 28 registers (the radix's values
-  // plus addresses and twiddles) and does not spill.
+  // so that each thread keeps about 2*qmax + 22 + REGX registers (the
+  // radix's values plus addresses and twiddles).
   template <int TARGET>
   static constexpr int min_blocks() {
-    const int fit = 65536 / (kThreads * (2 * Plan::qmax() + 22));
+    const int fit = 65536 / (kThreads * (2 * Plan::qmax() + 22 + REGX));
     const int b = TARGET < fit ? TARGET : fit;
     return b < 1 ? 1 : b;
   }

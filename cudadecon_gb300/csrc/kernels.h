@@ -76,6 +76,10 @@ struct FftLen {
   bool has_gx = false;
   FftDev gxdev;
   float2* d_twgx = nullptr;
+  // the generated z-pass plan of the length, if it has one
+  bool has_gz = false;
+  FftDev gzdev;
+  float2* d_twgz = nullptr;
   // the tensor-core plan of the length, if it has one
   bool has_tc = false;
   TcTables tc;

@@ -33,9 +33,11 @@
 #define CDX_XR_PLANS(F) F(1024, 2, 8, 16, 8)
 
 #define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 2) F(1024, 4) F(1620, 2)
-#define CDX_Y_PLANS(F) F(128, 16) F(256, 8) F(512, 4) F(1024, 4) CDX_GEN_Y_PLANS(F)
+// y entries: F(L, rows per block, extra registers of the launch bounds)
+#define CDX_Y_PLANS(F) F(128, 16, 0) F(256, 8, 0) F(512, 4, 0) F(1024, 4, 0) CDX_GEN_Y_PLANS(F)
 #define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
-// generated z plans: instantiated for radially averaged OTFs only
+// generated z plans (types SPZ<L>, twiddles FftLen::gzdev): F(L, columns
+// per block, extra registers); instantiated for radially averaged OTFs only
 #define CDX_Z_GEN_PLANS(F) CDX_GEN_Z_PLANS(F)
 
 namespace cdx {
@@ -48,6 +50,10 @@ CDX_SPLAN_LIST(CDX_DEF_SPLAN)
 CDX_GEN_X_SPLANS(CDX_DEF_GXPLAN)
 #undef CDX_DEF_GXPLAN
 
+#define CDX_DEF_GZPLAN(L, ...) using SPZ##L = SPlan<L, __VA_ARGS__>;
+CDX_GEN_Z_SPLANS(CDX_DEF_GZPLAN)
+#undef CDX_DEF_GZPLAN
+
 #define CDX_DEF_XRPLAN(L, P, ...) using SPR##L = SPlan<L, __VA_ARGS__>;
 CDX_XR_PLANS(CDX_DEF_XRPLAN)
 #undef CDX_DEF_XRPLAN
@@ -56,6 +62,10 @@ CDX_XR_PLANS(CDX_DEF_XRPLAN)
   static_assert(splan_rows_fit<SP##L, V>(), "row tile too small for the static plan of length " #L);
 CDX_X_PLANS(CDX_FIT_ROWS)
 #undef CDX_FIT_ROWS
+#define CDX_FIT_GX(L, P) \
+  static_assert(splan_rows_fit<SPX##L, P>(), "row tile too small for the x plan of length " #L);
+CDX_GEN_X_PAIRS(CDX_FIT_GX)
+#undef CDX_FIT_GX
 #define CDX_FIT_XR(L, P, ...) \
   static_assert(splan_rows_fit<SPR##L, P>(), "row tile too small for the x ratio plan of " #L);
 CDX_XR_PLANS(CDX_FIT_XR)
@@ -84,6 +94,35 @@ inline bool gx_radices(int L, std::vector<int>& rad) {
     return true;
     CDX_GEN_X_SPLANS(CDX_GX_CASE)
 #undef CDX_GX_CASE
+    default:
+      return false;
+  }
+}
+
+// Row pairs per block of the generated x-pass plan for length L (false when
+// it has none).
+inline bool gx_pairs(int L, int& pairs) {
+  switch (L) {
+#define CDX_GXP_CASE(LL, PP) \
+  case LL:                   \
+    pairs = PP;              \
+    return true;
+    CDX_GEN_X_PAIRS(CDX_GXP_CASE)
+#undef CDX_GXP_CASE
+    default:
+      return false;
+  }
+}
+
+// Radices of the generated z-pass plan for length L (false when it has none).
+inline bool gz_radices(int L, std::vector<int>& rad) {
+  switch (L) {
+#define CDX_GZ_CASE(LL, ...) \
+  case LL:                   \
+    rad = {__VA_ARGS__};     \
+    return true;
+    CDX_GEN_Z_SPLANS(CDX_GZ_CASE)
+#undef CDX_GZ_CASE
     default:
       return false;
   }

@@ -8,27 +8,44 @@ Writes csrc/static_plans_gen.cuh (the plan lists), csrc/x_gen_dispatch.h
 kernels of the generated x lengths, spread over several units so that the
 build compiles them in parallel).
 
-Plan choice: y and z: two radices of at most 32 points each (in
-registers), the most balanced pair, larger radix first; three radices when
-no such pair exists (343 = 7*7*7).  x: three radices, the most balanced
-triple, smallest last (the fused epilogues of the x passes run in the last
-stage, which then has a thread for every butterfly).  Tiles: y passes take
-2048 // L rows per block, z passes 16 columns, x passes the generic engine's
-row pairs (so the dot-product partials keep their size).  The z pass of
-these lengths is compiled for radially averaged OTFs; a full 3D OTF takes
-the generic engine.
+Each length has a short list of candidate plans (radix order, pencil batch
+-- rows, row pairs or columns per block -- and the register budget behind
+the launch bounds); candidate 0 is the heuristic choice:
 
-    python cudadecon_gb300/gen_plans.py     (rewrites the generated files)
+  y, z : the most balanced pair of radices of at most 32 points (in
+         registers), larger radix first; three radices when no such pair
+         exists (343 = 7*7*7).  y blocks take 2048 // L rows, z blocks 16
+         columns.  Candidates: half the rows (or 8 columns), the reversed
+         radix order, twice the rows (or 32 columns) where the block stays
+         within 1024 threads, 16 more registers per thread.
+  x    : the most balanced three radices, smallest last (the fused epilogues
+         of the x passes run in the last stage, which then has a thread for
+         every butterfly), with the generic engine's row pairs per block.
+         Candidates: half the row pairs, the two larger radices swapped, the
+         most balanced two-radix plan where its padded middle array fits the
+         tile, 16 more registers per thread.
+
+autotune.py times the candidates on the GPU and records the fastest per
+axis and length in tuned_plans.json, which this script then follows.
+
+    python cudadecon_gb300/gen_plans.py               (tuned, else candidate 0)
+    python cudadecon_gb300/gen_plans.py --column k    (candidate k everywhere,
+                                                       for the tuning builds)
 """
 
 from __future__ import annotations
 
+import argparse
+import json
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "csrc" / "static_plans_gen.cuh"
 XDISPATCH = HERE / "csrc" / "x_gen_dispatch.h"
+TUNED = HERE / "tuned_plans.json"
 X_UNITS = 12
+N_COLUMNS = 5
+REGX = 16
 
 REGISTERED = {32, 64, 100, 128, 256, 512, 756, 1024, 1620}
 X_RANGE = (128, 1024)
@@ -45,30 +62,24 @@ def smooth(n: int) -> bool:
     return n == 1
 
 
-def radices(L: int) -> list[int]:
+def lengths() -> dict[str, list[int]]:
+    def rng(r):
+        return [n for n in range(r[0], r[1] + 1) if smooth(n) and n not in REGISTERED]
+    return {"x": rng(X_RANGE), "y": rng(Y_RANGE), "z": rng(Z_RANGE)}
+
+
+def radices2(L: int) -> list[int] | None:
+    """The most balanced pair of radices <= 32 (larger first), or None."""
     best = None
     for a in range(2, 33):
         b, r = divmod(L, a)
         if r == 0 and 2 <= b <= 32 and (best is None or max(a, b) < max(best)):
             best = (max(a, b), min(a, b))
-    if best:
-        return list(best)
-    best3 = None
-    for a in range(2, 33):
-        if L % a:
-            continue
-        for b in range(2, 33):
-            c, r = divmod(L // a, b)
-            if (L // a) % b == 0 and 2 <= c <= 32:
-                t = sorted((a, b, c), reverse=True)
-                if best3 is None or t[0] < best3[0]:
-                    best3 = t
-    if best3 is None:
-        raise ValueError(f"no plan of radices <= 32 for {L}")
-    return best3
+    return list(best) if best else None
 
 
 def radices3(L: int) -> list[int]:
+    """The most balanced triple of radices <= 32, in descending order."""
     best = None
     for a in range(2, 33):
         if L % a:
@@ -85,6 +96,11 @@ def radices3(L: int) -> list[int]:
     return best[1]
 
 
+def radices(L: int) -> list[int]:
+    """y/z plans: a pair where one exists, else three radices."""
+    return radices2(L) or radices3(L)
+
+
 def x_pairs(nx: int) -> int:
     """Row pairs per x tile of the generic engine (x_pairs, decon_common.cuh)."""
     p = min(8, 8192 // nx)
@@ -93,7 +109,74 @@ def x_pairs(nx: int) -> int:
     return max(p, 1)
 
 
-def x_units(xs: list[int]) -> None:
+def threads(L: int, rad: list[int], batch: int) -> int:
+    """Threads of a block (splan_threads, fft_static.cuh)."""
+    t = batch * (L // min(rad))
+    return (t + 31) // 32 * 32
+
+
+def spad_size(n: int) -> int:
+    return n + (n >> 4) + 1
+
+
+def x_fits(L: int, rad: list[int], P: int) -> bool:
+    """A two-radix plan's padded middle array must fit the padded row tile
+    the x launchers allocate (splan_rows_fit, fft_static.cuh)."""
+    if threads(L, rad, P) > MAX_THREADS:
+        return False
+    if len(rad) == 2:
+        return P * rad[1] * (rad[0] + 1) <= spad_size(P * L)
+    return True
+
+
+def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
+    """Candidate (radices, batch, extra registers) of one length, candidate 0
+    first."""
+    out: list[tuple[list[int], int, int]] = []
+
+    def add(rad, b, rx=0):
+        if (list(rad), b, rx) in out:
+            return
+        if axis == "x" and not x_fits(L, rad, b):
+            return
+        if axis != "x" and threads(L, rad, b) > MAX_THREADS:
+            return
+        out.append((list(rad), b, rx))
+
+    if axis == "x":
+        base, P = radices3(L), x_pairs(L)
+        add(base, P)
+        add(base, max(1, P // 2))
+        add([base[1], base[0], base[2]], P)
+        pair = radices2(L)
+        if pair:
+            add(pair, P)
+        add(base, P, REGX)
+    else:
+        base = radices(L)
+        b = max(1, 2048 // L) if axis == "y" else Z_COLS
+        add(base, b)
+        add(base, max(1, b // 2))
+        add(list(reversed(base)), b)
+        add(base, 2 * b)
+        add(base, b, REGX)
+    assert out, f"no plan within {MAX_THREADS} threads for {axis} length {L}"
+    return out
+
+
+def choose(axis: str, L: int, column: int | None, tuned: dict) -> tuple[list[int], int, int]:
+    c = candidates(axis, L)
+    if column is not None:
+        return c[column] if column < len(c) else c[0]
+    t = tuned.get(axis, {}).get(str(L))
+    if t:
+        pick = (t["radices"], t["batch"], t.get("regx", 0))
+        if pick in c:
+            return pick
+    return c[0]
+
+
+def x_units(xs: list[int], xplans: dict[int, tuple[list[int], int, int]]) -> None:
     units = [xs[k::X_UNITS] for k in range(X_UNITS)]
     kinds = {
         "fwd": ("const float* X, float* Xm1, const float* lam, int predict, float2* S",
@@ -131,53 +214,58 @@ def x_units(xs: list[int]) -> None:
                        f"cudaStream_t st, bool* done) {{")
             out.append("  switch (g.nx) {")
             for L in lens:
-                P = x_pairs(L)
+                _, P, rx = xplans[L]
                 c = call.replace("PP", str(P))
                 out.append(f"    case {L}:")
                 out.append("      *done = true;")
-                out.append(f"      return {go}<StaticRunner<SPX{L}, {P}, false>>({c}, "
-                           f"splan_threads<SPX{L}, {P}>(), st);")
+                out.append(f"      return {go}<StaticRunner<SPX{L}, {P}, false, false, {rx}>>("
+                           f"{c}, splan_threads<SPX{L}, {P}>(), st);")
             out += ["    default:", "      return 0;", "  }", "}", ""]
         out += ["}  // namespace cdx", ""]
         (HERE / "csrc" / f"decon_x_gen_{k}.cu").write_text("\n".join(out))
 
 
-def main() -> None:
-    xs = [n for n in range(X_RANGE[0], X_RANGE[1] + 1) if smooth(n) and n not in REGISTERED]
-    ys = [n for n in range(Y_RANGE[0], Y_RANGE[1] + 1) if smooth(n) and n not in REGISTERED]
-    zs = [n for n in range(Z_RANGE[0], Z_RANGE[1] + 1) if smooth(n) and n not in REGISTERED]
-    plans = {}
-    for L in sorted(set(ys) | set(zs)):
-        plans[L] = radices(L)
-    # x lengths have plans of their own (SPX<L>, three radices)
-    xplans = {L: radices3(L) for L in xs}
-    for L in xs:
-        assert x_pairs(L) * L // min(xplans[L]) <= MAX_THREADS, L
-    yv = {L: max(1, 2048 // L) for L in ys}
-    for L in ys:
-        assert yv[L] * L // min(plans[L]) <= MAX_THREADS, L
-    for L in zs:
-        assert Z_COLS * L // min(plans[L]) <= MAX_THREADS, L
+def generate(column: int | None = None) -> dict[str, dict[int, tuple[list[int], int, int]]]:
+    """Write the generated sources; returns the chosen plans per axis."""
+    tuned = json.loads(TUNED.read_text()) if column is None and TUNED.exists() else {}
+    lens = lengths()
+    plans = {a: {L: choose(a, L, column, tuned) for L in lens[a]} for a in lens}
+    src = "tuned_plans.json" if tuned else ("candidate column %d" % column if column is not None
+                                             else "candidate 0")
     lines = [
         "// Generated by cudadecon_gb300/gen_plans.py (do not edit): compile-time",
         "// plans for the 2,3,5,7-smooth x lengths in [128, 1024], y lengths in",
         "// [128, 512] and z lengths in [32, 160] outside the hand-tuned registry of",
-        "// static_plans.cuh (x plans are types of their own, SPX<L>).",
+        "// static_plans.cuh; x plans are types SPX<L>, z plans SPZ<L>, y plans",
+        f"// SP<L>.  Plans from {src}.",
         "#pragma once",
         "",
-        "#define CDX_GEN_SPLANS(F) \\",
     ]
-    lines += [f"  F({L}, {', '.join(map(str, r))}) \\" for L, r in plans.items()]
-    lines += ["", "#define CDX_GEN_X_SPLANS(F) \\"]
-    lines += [f"  F({L}, {', '.join(map(str, r))}) \\" for L, r in xplans.items()]
-    lines += ["", "#define CDX_GEN_Y_PLANS(F) \\"]
-    lines += [f"  F({L}, {yv[L]}) \\" for L in ys]
-    lines += ["", "#define CDX_GEN_Z_PLANS(F) \\"]
-    lines += [f"  F({L}, {Z_COLS}) \\" for L in zs]
-    lines += [""]
+
+    def block(name, items):
+        return [f"#define {name}(F) \\"] + [f"  F({i}) \\" for i in items] + [""]
+
+    lines += block("CDX_GEN_SPLANS", [f"{L}, {', '.join(map(str, r))}"
+                                      for L, (r, _, _) in plans["y"].items()])
+    lines += block("CDX_GEN_Z_SPLANS", [f"{L}, {', '.join(map(str, r))}"
+                                        for L, (r, _, _) in plans["z"].items()])
+    lines += block("CDX_GEN_X_SPLANS", [f"{L}, {', '.join(map(str, r))}"
+                                        for L, (r, _, _) in plans["x"].items()])
+    lines += block("CDX_GEN_X_PAIRS", [f"{L}, {P}" for L, (_, P, _) in plans["x"].items()])
+    lines += block("CDX_GEN_Y_PLANS", [f"{L}, {V}, {rx}" for L, (_, V, rx) in plans["y"].items()])
+    lines += block("CDX_GEN_Z_PLANS", [f"{L}, {W}, {rx}" for L, (_, W, rx) in plans["z"].items()])
     OUT.write_text("\n".join(lines) + "\n")
-    x_units(xs)
-    print(f"{OUT}: {len(plans)} y/z plans ({len(ys)} y, {len(zs)} z lengths), {len(xplans)} x plans")
+    x_units(lens["x"], plans["x"])
+    return plans
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--column", type=int, default=None,
+                    help="use candidate COLUMN for every length (tuning builds)")
+    a = ap.parse_args()
+    plans = generate(a.column)
+    print(f"{OUT}: {len(plans['y'])} y, {len(plans['z'])} z and {len(plans['x'])} x plans")
 
 
 if __name__ == "__main__":
