@@ -15,10 +15,10 @@ int xgen_fwd_4(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX224, 8>(), st);
     case 315:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX315, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX315, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX405, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX405, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
       return x_fwd_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX540, 4>(), st);
@@ -43,10 +43,10 @@ int xgen_ratio_4(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX224, 8>(), st);
     case 315:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX315, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX315, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX405, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX405, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
       return x_ratio_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX540, 4>(), st);
@@ -71,10 +71,10 @@ int xgen_update_4(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX224, 8>(), st);
     case 315:
       *done = true;
-      return x_update_go<StaticRunner<SPX315, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX315, 8>(), st);
+      return x_update_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_update_go<StaticRunner<SPX405, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX405, 8>(), st);
+      return x_update_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
       return x_update_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX540, 4>(), st);

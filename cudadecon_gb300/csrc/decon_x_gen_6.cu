@@ -15,19 +15,19 @@ int xgen_fwd_6(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX324, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX324, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX432, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX432, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX567, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX567, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
       return x_fwd_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX720, 4>(), st);
     case 896:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX896, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX896, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }
@@ -43,19 +43,19 @@ int xgen_ratio_6(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX324, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX324, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX432, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX432, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX567, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX567, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
       return x_ratio_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX720, 4>(), st);
     case 896:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX896, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX896, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }
@@ -71,19 +71,19 @@ int xgen_update_6(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_update_go<StaticRunner<SPX324, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX324, 8>(), st);
+      return x_update_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_update_go<StaticRunner<SPX432, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX432, 8>(), st);
+      return x_update_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
-      return x_update_go<StaticRunner<SPX567, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX567, 4>(), st);
+      return x_update_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
       return x_update_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX720, 4>(), st);
     case 896:
       *done = true;
-      return x_update_go<StaticRunner<SPX896, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX896, 4>(), st);
+      return x_update_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }

@@ -12,22 +12,22 @@ int xgen_fwd_7(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX168, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX168, 8>(), st);
     case 243:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX243, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX243, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX243, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX243, 4>(), st);
     case 336:
       *done = true;
       return x_fwd_go<StaticRunner<SPX336, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX336, 8>(), st);
     case 441:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX441, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX441, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX441, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX576, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX576, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX576, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_fwd_go<StaticRunner<SPX729, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX729, 4>(), st);
     case 900:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX900, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX900, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX900, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX900, 2>(), st);
     default:
       return 0;
   }
@@ -40,22 +40,22 @@ int xgen_ratio_7(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX168, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX168, 8>(), st);
     case 243:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX243, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX243, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX243, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX243, 4>(), st);
     case 336:
       *done = true;
       return x_ratio_go<StaticRunner<SPX336, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX336, 8>(), st);
     case 441:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX441, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX441, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX441, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX576, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX576, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX576, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_ratio_go<StaticRunner<SPX729, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX729, 4>(), st);
     case 900:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX900, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX900, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX900, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX900, 2>(), st);
     default:
       return 0;
   }
@@ -68,22 +68,22 @@ int xgen_update_7(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX168, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX168, 8>(), st);
     case 243:
       *done = true;
-      return x_update_go<StaticRunner<SPX243, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX243, 8>(), st);
+      return x_update_go<StaticRunner<SPX243, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX243, 4>(), st);
     case 336:
       *done = true;
       return x_update_go<StaticRunner<SPX336, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX336, 8>(), st);
     case 441:
       *done = true;
-      return x_update_go<StaticRunner<SPX441, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX441, 8>(), st);
+      return x_update_go<StaticRunner<SPX441, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_update_go<StaticRunner<SPX576, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX576, 4>(), st);
+      return x_update_go<StaticRunner<SPX576, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_update_go<StaticRunner<SPX729, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX729, 4>(), st);
     case 900:
       *done = true;
-      return x_update_go<StaticRunner<SPX900, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX900, 4>(), st);
+      return x_update_go<StaticRunner<SPX900, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX900, 2>(), st);
     default:
       return 0;
   }

@@ -17,13 +17,17 @@ the launch bounds); candidate 0 is the heuristic choice:
          exists (343 = 7*7*7).  y blocks take 2048 // L rows, z blocks 16
          columns.  Candidates: half the rows (or 8 columns), the reversed
          radix order, twice the rows (or 32 columns) where the block stays
-         within 1024 threads, 16 more registers per thread.
+         within 1024 threads, 16 more registers per thread, and three
+         radices (the most balanced triple) with the full and half batch:
+         an unbalanced pair such as 125 = 25*5 leaves most threads idle in
+         its large-radix stage.
   x    : the most balanced three radices, smallest last (the fused epilogues
          of the x passes run in the last stage, which then has a thread for
          every butterfly), with the generic engine's row pairs per block.
          Candidates: half the row pairs, the two larger radices swapped, the
          most balanced two-radix plan where its padded middle array fits the
-         tile, 16 more registers per thread.
+         tile, 16 more registers per thread, a quarter of the row pairs, and
+         the swapped radices with half the row pairs.
 
 autotune.py times the candidates on the GPU and records the fastest per
 axis and length in tuned_plans.json, which this script then follows.
@@ -44,7 +48,7 @@ OUT = HERE / "csrc" / "static_plans_gen.cuh"
 XDISPATCH = HERE / "csrc" / "x_gen_dispatch.h"
 TUNED = HERE / "tuned_plans.json"
 X_UNITS = 12
-N_COLUMNS = 5
+N_COLUMNS = 7
 REGX = 16
 
 REGISTERED = {32, 64, 100, 128, 256, 512, 756, 1024, 1620}
@@ -145,13 +149,16 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
 
     if axis == "x":
         base, P = radices3(L), x_pairs(L)
+        swapped = [base[1], base[0], base[2]]
         add(base, P)
         add(base, max(1, P // 2))
-        add([base[1], base[0], base[2]], P)
+        add(swapped, P)
         pair = radices2(L)
         if pair:
             add(pair, P)
         add(base, P, REGX)
+        add(base, max(1, P // 4))
+        add(swapped, max(1, P // 2))
     else:
         base = radices(L)
         b = max(1, 2048 // L) if axis == "y" else Z_COLS
@@ -160,6 +167,14 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
         add(list(reversed(base)), b)
         add(base, 2 * b)
         add(base, b, REGX)
+        if len(base) == 2:
+            try:
+                tri = radices3(L)
+            except ValueError:
+                tri = None
+            if tri:
+                add(tri, b)
+                add(tri, max(1, b // 2))
     assert out, f"no plan within {MAX_THREADS} threads for {axis} length {L}"
     return out
 
