@@ -2,7 +2,7 @@
 
 Every length of the batched workloads' ranges has a few candidate plans
 (gen_plans.candidates): radix order, pencil batch (y rows, z columns or x
-row pairs per block) and register budget.  Plans are compile-time types,
+row pairs per block), register budget and stage-layout padding.  Plans are compile-time types,
 so the tuner builds the library once per candidate column (column k =
 candidate k of every length, candidate 0 where a length has fewer) in a
 scratch copy of the package, runs one synthetic stack per length through cdx_RL_device with the
@@ -78,8 +78,8 @@ def select(times_by_column: list[dict[str, dict[int, float]]], cands, margin: fl
             best = min(ms, key=ms.get)
             if ms[best] > ms[0] * (1.0 - margin):
                 best = 0
-            rad, batch, regx = c[best]
-            res[axis][str(L)] = {"radices": rad, "batch": batch, "regx": regx,
+            rad, batch, regx, pads = c[best]
+            res[axis][str(L)] = {"radices": rad, "batch": batch, "regx": regx, "pads": pads,
                                  "candidate": best,
                                  "ms": {str(k): round(v, 5) for k, v in ms.items()}}
     return res

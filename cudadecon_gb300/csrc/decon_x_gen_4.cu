@@ -9,25 +9,25 @@ int xgen_fwd_4(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
   switch (g.nx) {
     case 150:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX150, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX150, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX150, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX150, 8>(), st);
     case 224:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX224, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX224, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX224, 4>(), st);
     case 315:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX315, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX315, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX405, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX405, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX540, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX540, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX540, 4>(), st);
     case 686:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX686, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX686, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX686, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX686, 4>(), st);
     case 875:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX875, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX875, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX875, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX875, 2>(), st);
     default:
       return 0;
   }
@@ -37,25 +37,25 @@ int xgen_ratio_4(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
   switch (g.nx) {
     case 150:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX150, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX150, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX150, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX150, 8>(), st);
     case 224:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX224, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX224, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX224, 4>(), st);
     case 315:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX315, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX315, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX405, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX405, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX540, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX540, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX540, 4>(), st);
     case 686:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX686, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX686, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX686, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX686, 4>(), st);
     case 875:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX875, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX875, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX875, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX875, 2>(), st);
     default:
       return 0;
   }
@@ -65,25 +65,25 @@ int xgen_update_4(const Geom& g, const FftLen& fx, const float2* S, const float*
   switch (g.nx) {
     case 150:
       *done = true;
-      return x_update_go<StaticRunner<SPX150, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX150, 8>(), st);
+      return x_update_go<StaticRunner<SPX150, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX150, 8>(), st);
     case 224:
       *done = true;
-      return x_update_go<StaticRunner<SPX224, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX224, 8>(), st);
+      return x_update_go<StaticRunner<SPX224, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX224, 4>(), st);
     case 315:
       *done = true;
-      return x_update_go<StaticRunner<SPX315, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX315, 4>(), st);
+      return x_update_go<StaticRunner<SPX315, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX315, 4>(), st);
     case 405:
       *done = true;
-      return x_update_go<StaticRunner<SPX405, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX405, 4>(), st);
+      return x_update_go<StaticRunner<SPX405, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX405, 4>(), st);
     case 540:
       *done = true;
-      return x_update_go<StaticRunner<SPX540, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX540, 4>(), st);
+      return x_update_go<StaticRunner<SPX540, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX540, 4>(), st);
     case 686:
       *done = true;
-      return x_update_go<StaticRunner<SPX686, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX686, 4>(), st);
+      return x_update_go<StaticRunner<SPX686, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX686, 4>(), st);
     case 875:
       *done = true;
-      return x_update_go<StaticRunner<SPX875, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX875, 4>(), st);
+      return x_update_go<StaticRunner<SPX875, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX875, 2>(), st);
     default:
       return 0;
   }

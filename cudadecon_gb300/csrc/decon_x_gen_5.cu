@@ -9,25 +9,25 @@ int xgen_fwd_5(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
   switch (g.nx) {
     case 160:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX160, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX160, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX225, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX225, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX320, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX320, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX320, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX320, 8>(), st);
     case 420:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX420, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX420, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX420, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX420, 8>(), st);
     case 560:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX560, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX560, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX560, 2>(), st);
     case 700:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX700, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX700, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX700, 4>(), st);
     case 882:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX882, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX882, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX882, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX882, 2>(), st);
     default:
       return 0;
   }
@@ -37,25 +37,25 @@ int xgen_ratio_5(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
   switch (g.nx) {
     case 160:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX160, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX160, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX225, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX225, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX320, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX320, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX320, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX320, 8>(), st);
     case 420:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX420, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX420, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX420, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX420, 8>(), st);
     case 560:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX560, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX560, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX560, 2>(), st);
     case 700:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX700, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX700, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX700, 4>(), st);
     case 882:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX882, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX882, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX882, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX882, 2>(), st);
     default:
       return 0;
   }
@@ -65,25 +65,25 @@ int xgen_update_5(const Geom& g, const FftLen& fx, const float2* S, const float*
   switch (g.nx) {
     case 160:
       *done = true;
-      return x_update_go<StaticRunner<SPX160, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX160, 8>(), st);
+      return x_update_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_update_go<StaticRunner<SPX225, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX225, 4>(), st);
+      return x_update_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
-      return x_update_go<StaticRunner<SPX320, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX320, 8>(), st);
+      return x_update_go<StaticRunner<SPX320, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX320, 8>(), st);
     case 420:
       *done = true;
-      return x_update_go<StaticRunner<SPX420, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX420, 4>(), st);
+      return x_update_go<StaticRunner<SPX420, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX420, 8>(), st);
     case 560:
       *done = true;
-      return x_update_go<StaticRunner<SPX560, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX560, 2>(), st);
+      return x_update_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX560, 2>(), st);
     case 700:
       *done = true;
-      return x_update_go<StaticRunner<SPX700, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX700, 4>(), st);
+      return x_update_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX700, 4>(), st);
     case 882:
       *done = true;
-      return x_update_go<StaticRunner<SPX882, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX882, 2>(), st);
+      return x_update_go<StaticRunner<SPX882, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX882, 2>(), st);
     default:
       return 0;
   }

@@ -9,25 +9,25 @@ int xgen_fwd_6(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
   switch (g.nx) {
     case 162:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX162, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX162, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX240, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX324, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX324, 8>(), st);
     case 432:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX432, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX432, 8>(), st);
     case 567:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX567, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX720, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX720, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX720, 2>(), st);
     case 896:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX896, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX896, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }
@@ -37,25 +37,25 @@ int xgen_ratio_6(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
   switch (g.nx) {
     case 162:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX162, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX162, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX240, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX324, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX324, 8>(), st);
     case 432:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX432, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX432, 8>(), st);
     case 567:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX567, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX720, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX720, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX720, 2>(), st);
     case 896:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX896, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX896, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }
@@ -65,25 +65,25 @@ int xgen_update_6(const Geom& g, const FftLen& fx, const float2* S, const float*
   switch (g.nx) {
     case 162:
       *done = true;
-      return x_update_go<StaticRunner<SPX162, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX162, 8>(), st);
+      return x_update_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_update_go<StaticRunner<SPX240, 8, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX240, 8>(), st);
+      return x_update_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX240, 8>(), st);
     case 324:
       *done = true;
-      return x_update_go<StaticRunner<SPX324, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX324, 4>(), st);
+      return x_update_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX324, 8>(), st);
     case 432:
       *done = true;
-      return x_update_go<StaticRunner<SPX432, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX432, 4>(), st);
+      return x_update_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX432, 8>(), st);
     case 567:
       *done = true;
-      return x_update_go<StaticRunner<SPX567, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX567, 2>(), st);
+      return x_update_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX567, 2>(), st);
     case 720:
       *done = true;
-      return x_update_go<StaticRunner<SPX720, 4, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX720, 4>(), st);
+      return x_update_go<StaticRunner<SPX720, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX720, 2>(), st);
     case 896:
       *done = true;
-      return x_update_go<StaticRunner<SPX896, 2, false, false, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX896, 2>(), st);
+      return x_update_go<StaticRunner<SPX896, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX896, 2>(), st);
     default:
       return 0;
   }

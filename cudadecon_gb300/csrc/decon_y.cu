@@ -37,10 +37,10 @@ static int y_go(const Geom& g, const FftDev& f, float2* S, int V, int T, cudaStr
 template <bool INV>
 static int y_dispatch(const Geom& g, const FftLen& fy, float2* S, cudaStream_t st) {
   if (fy.has_static) switch (g.ny) {
-#define CDX_CASE(L, VV, RR)                                                           \
+#define CDX_CASE(L, VV, RR, B0, B1)                                                   \
   case L:                                                                             \
-    return y_go<INV, StaticRunner<SP##L, VV, false, false, RR>>(g, fy.sdev, S, VV,     \
-                                                                splan_threads<SP##L, VV>(), st);
+    return y_go<INV, StaticRunner<SP##L, VV, false, false, RR, B0, B1>>(               \
+        g, fy.sdev, S, VV, splan_threads<SP##L, VV>(), st);
       CDX_Y_PLANS(CDX_CASE)
 #undef CDX_CASE
       default:

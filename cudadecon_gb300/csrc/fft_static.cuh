@@ -104,6 +104,28 @@ struct NatIO {
   __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[v * vs + e] = x; }
 };
 
+// A row tile with one float2 of padding after every B (B = 0: none): the
+// layout between two stages of a three-radix row plan.  The stage before it
+// writes at stride Q0 (first stage) or in runs of the span, which for even
+// radices or short spans puts several threads of a half-warp on the same
+// bank; the padding spreads them.  B is chosen per plan and boundary from a
+// bank model of both stages' accesses (gen_plans.py), and B >= 16 keeps the
+// tile within the padded size spad_size(V*L) the launchers allocate.
+template <int B>
+struct PadIO {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  static_assert(B == 0 || B >= 16, "padding period below the allocated slack");
+  float2* sm;
+  int vs;
+  __device__ __forceinline__ int ix(int v, int e) const {
+    const int t = v * vs + e;
+    return B > 0 ? t + t / B : t;
+  }
+  __device__ __forceinline__ float2 ld(int v, int e) const { return sm[ix(v, e)]; }
+  __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[ix(v, e)] = x; }
+};
+
 // Float2s of the middle layout of a two-radix plan over V vectors.
 template <class Plan, int V>
 constexpr int splan_mid_size() {
@@ -234,7 +256,8 @@ __device__ __forceinline__ void sfft2_cols(const float2* stw, float2* tile, cons
 // Full transform; same contract as fft_run (fft_engine.cuh): the first stage
 // reads with ld0, the last writes with stL, the stages between work in place
 // on io; ends with a barrier when stL writes shared memory.
-template <class Plan, bool INV, int V, bool VFAST, bool GTW, class IO, class Ld0, class StL>
+template <class Plan, bool INV, int V, bool VFAST, bool GTW, int B0, int B1, class IO, class Ld0,
+          class StL>
 __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const Ld0& ld0,
                                          const StL& stL) {
   constexpr int L = Plan::kL;
@@ -246,6 +269,15 @@ __device__ __forceinline__ void sfft_run(const float2* stw, const IO& io, const 
     sfft2_cols<Plan, INV, V>(stw, io.sm, ld0, stL);
   } else if constexpr (N == 1) {
     sstage<L, Plan::q(0), 1, INV, V, VFAST, true, StL::kSmem, Ld0, StL, GTW>(stw, ld0, stL);
+  } else if constexpr (N == 3 && !VFAST && (B0 > 0 || B1 > 0)) {
+    // three radices over row tiles with padded layouts between the stages
+    const PadIO<B0> m0{io.sm, io.vs};
+    const PadIO<B1> m1{io.sm, io.vs};
+    sstage<L, Plan::q(0), 1, INV, V, false, Ld0::kSmem, true, Ld0, PadIO<B0>, GTW>(stw, ld0, m0);
+    sstage<L, Plan::q(1), Plan::ns(1), INV, V, false, true, true, PadIO<B0>, PadIO<B1>, GTW>(
+        stw, m0, m1);
+    sstage<L, Plan::q(2), Plan::ns(2), INV, V, false, StL::kSmem, StL::kSmem, PadIO<B1>, StL,
+           GTW>(stw, m1, stL);
   } else {
     // three or more radices: the stages between work in place on the
     // natural-order tile (unit-stride reads; the first stage writes at
@@ -288,8 +320,9 @@ struct GenericRunner {
 // read-only cache) instead of a shared-memory copy, which saves the kernel
 // L float2s of shared memory.  REGX: registers per thread added to the
 // estimate behind the launch bounds (fewer blocks per SM, more registers
-// for each thread).
-template <class Plan, int V, bool VFAST, bool GTW = false, int REGX = 0>
+// for each thread).  B0, B1: padding periods of the layouts after the first
+// and the second stage of a three-radix row plan (PadIO; 0 = natural).
+template <class Plan, int V, bool VFAST, bool GTW = false, int REGX = 0, int B0 = 0, int B1 = 0>
 struct StaticRunner {
   static constexpr bool kStatic = true;
   static constexpr int kV = V;
@@ -310,6 +343,7 @@ struct StaticRunner {
   static constexpr int kTileF2 = [] {
     int m = splan_mid_size<Plan, V>();
     if (V * Plan::kL > m) m = V * Plan::kL;
+    if ((B0 > 0 || B1 > 0) && spad_size(V * Plan::kL) > m) m = spad_size(V * Plan::kL);
     if (2 * (Plan::kL / 2 + 1) * V > m) m = 2 * (Plan::kL / 2 + 1) * V;
     return m + (m & 1);
   }();
@@ -319,7 +353,7 @@ struct StaticRunner {
   template <bool INV, class IO, class Ld0, class StL>
   __device__ __forceinline__ static void run(const FftDev&, int, float, bool, const float2* stw,
                                              const IO& io, const Ld0& ld0, const StL& stL) {
-    sfft_run<Plan, INV, V, VFAST, GTW>(stw, io, ld0, stL);
+    sfft_run<Plan, INV, V, VFAST, GTW, B0, B1>(stw, io, ld0, stL);
   }
 };
 

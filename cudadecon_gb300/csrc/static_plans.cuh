@@ -33,8 +33,10 @@
 #define CDX_XR_PLANS(F) F(1024, 2, 8, 16, 8)
 
 #define CDX_X_PLANS(F) F(128, 8) F(256, 8) F(512, 4) F(756, 2) F(1024, 4) F(1620, 2)
-// y entries: F(L, rows per block, extra registers of the launch bounds)
-#define CDX_Y_PLANS(F) F(128, 16, 0) F(256, 8, 0) F(512, 4, 0) F(1024, 4, 0) CDX_GEN_Y_PLANS(F)
+// y entries: F(L, rows per block, extra registers of the launch bounds,
+// padding periods of the two stage layouts of a three-radix plan)
+#define CDX_Y_PLANS(F) \
+  F(128, 16, 0, 0, 0) F(256, 8, 0, 0, 0) F(512, 4, 0, 0, 0) F(1024, 4, 0, 0, 0) CDX_GEN_Y_PLANS(F)
 #define CDX_Z_PLANS(F) F(32, 16) F(64, 16) F(100, 16) F(128, 16) F(256, 16)
 // generated z plans (types SPZ<L>, twiddles FftLen::gzdev): F(L, columns
 // per block, extra registers); instantiated for radially averaged OTFs only

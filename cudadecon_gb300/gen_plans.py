@@ -9,8 +9,9 @@ kernels of the generated x lengths, spread over several units so that the
 build compiles them in parallel).
 
 Each length has a short list of candidate plans (radix order, pencil batch
--- rows, row pairs or columns per block -- and the register budget behind
-the launch bounds); candidate 0 is the heuristic choice:
+-- rows, row pairs or columns per block -- the register budget behind the
+launch bounds, and for three-radix row plans the padding of the layouts
+between the stages); candidate 0 is the heuristic choice:
 
   y, z : the most balanced pair of radices of at most 32 points (in
          registers), larger radix first; three radices when no such pair
@@ -29,6 +30,12 @@ the launch bounds); candidate 0 is the heuristic choice:
          tile, 16 more registers per thread, a quarter of the row pairs, and
          the swapped radices with half the row pairs.
 
+Padding (x and y plans of three radices): each layout between two stages
+gets one float2 of padding after every B, with B in PAD_CHOICES picked by a
+model of the shared-memory bank conflicts of the stage that writes it and
+the stage that reads it (smem_pads); every candidate carries its model
+padding, and one more candidate is candidate 0 without it.
+
 autotune.py times the candidates on the GPU and records the fastest per
 axis and length in tuned_plans.json, which this script then follows.
 
@@ -40,16 +47,20 @@ axis and length in tuned_plans.json, which this script then follows.
 from __future__ import annotations
 
 import argparse
+import functools
 import json
 from pathlib import Path
+
+import numpy as np
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "csrc" / "static_plans_gen.cuh"
 XDISPATCH = HERE / "csrc" / "x_gen_dispatch.h"
 TUNED = HERE / "tuned_plans.json"
 X_UNITS = 12
-N_COLUMNS = 7
+N_COLUMNS = 8
 REGX = 16
+PAD_CHOICES = (0, 16, 20, 24, 28, 32, 48, 64, 96, 128)
 
 REGISTERED = {32, 64, 100, 128, 256, 512, 756, 1024, 1620}
 X_RANGE = (128, 1024)
@@ -133,19 +144,83 @@ def x_fits(L: int, rad: list[int], P: int) -> bool:
     return True
 
 
-def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
-    """Candidate (radices, batch, extra registers) of one length, candidate 0
-    first."""
-    out: list[tuple[list[int], int, int]] = []
+def _wavefronts64(addr: np.ndarray) -> int:
+    """Shared-memory wavefronts of 8-byte accesses: addr (..., 32) float2
+    indices of one warp's threads (-1: inactive); each half-warp is one
+    request whose wavefronts are the most distinct words on one bank."""
+    a = addr.reshape(-1, 16)
+    act = np.concatenate([a >= 0, a >= 0], axis=1)
+    words = np.where(act, np.concatenate([2 * a, 2 * a + 1], axis=1), -1)
+    words.sort(axis=1)
+    uniq = np.ones_like(words, dtype=bool)
+    uniq[:, 1:] = words[:, 1:] != words[:, :-1]
+    uniq &= words >= 0
+    g = np.broadcast_to(np.arange(words.shape[0])[:, None], words.shape)
+    cnt = np.zeros((words.shape[0], 32), dtype=np.int64)
+    np.add.at(cnt, (g[uniq], words[uniq] % 32), 1)
+    return int(cnt.max(axis=1).sum())
 
-    def add(rad, b, rx=0):
-        if (list(rad), b, rx) in out:
-            return
+
+def boundary_wavefronts(L: int, rad: list[int], V: int, s: int, B: int) -> int:
+    """Wavefronts of the stores of stage s and the loads of stage s + 1 of a
+    row plan (sstage in fft_static.cuh: thread b owns butterfly j of vector
+    v; loads at j + r L/Q, stores at (j - k) Q + k + r Ns with k = j mod
+    Ns) through the layout padded every B float2s."""
+    T = threads(L, rad, V)
+    b = np.arange(T)
+    ns = int(np.prod(rad[:s])) if s else 1
+    tot = 0
+    for kind, Q, nsk in (("st", rad[s], ns), ("ld", rad[s + 1], ns * rad[s])):
+        LR = L // Q
+        v, j = np.divmod(b, LR)
+        r = np.arange(Q)[:, None]
+        if kind == "ld":
+            e = j[None, :] + r * LR
+        else:
+            k = j % nsk
+            e = ((j - k) * Q + k)[None, :] + r * nsk
+        t = v[None, :] * L + e
+        if B:
+            t = t + t // B
+        t = np.where(b[None, :] < V * LR, t, -1)
+        tot += _wavefronts64(t.reshape(Q, -1, 32))
+    return tot
+
+
+def smem_pads(L: int, rad: list[int], V: int) -> list[int]:
+    """Padding periods of the two layouts between the stages of a
+    three-radix row plan: the fewest modelled wavefronts, 0 (natural) unless
+    a padding saves at least 5%."""
+    return list(_smem_pads(L, tuple(rad), V))
+
+
+@functools.lru_cache(maxsize=None)
+def _smem_pads(L: int, rad: tuple[int, ...], V: int) -> tuple[int, int]:
+    if len(rad) != 3:
+        return (0, 0)
+    out = []
+    for s in range(2):
+        cost = {B: boundary_wavefronts(L, list(rad), V, s, B) for B in PAD_CHOICES}
+        best = min(cost, key=lambda B: (cost[B], B))
+        out.append(best if cost[best] <= 0.95 * cost[0] else 0)
+    return tuple(out)
+
+
+def candidates(axis: str, L: int) -> list[tuple[list[int], int, int, list[int]]]:
+    """Candidate (radices, batch, extra registers, paddings) of one length,
+    candidate 0 first."""
+    out: list[tuple[list[int], int, int, list[int]]] = []
+
+    def add(rad, b, rx=0, padded=True):
+        rad = list(rad)
         if axis == "x" and not x_fits(L, rad, b):
             return
         if axis != "x" and threads(L, rad, b) > MAX_THREADS:
             return
-        out.append((list(rad), b, rx))
+        pads = smem_pads(L, rad, b) if padded and axis != "z" else [0, 0]
+        c = (rad, b, rx, pads)
+        if c not in out:
+            out.append(c)
 
     if axis == "x":
         base, P = radices3(L), x_pairs(L)
@@ -159,6 +234,7 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
         add(base, P, REGX)
         add(base, max(1, P // 4))
         add(swapped, max(1, P // 2))
+        add(base, P, padded=False)
     else:
         base = radices(L)
         b = max(1, 2048 // L) if axis == "y" else Z_COLS
@@ -175,23 +251,25 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int]]:
             if tri:
                 add(tri, b)
                 add(tri, max(1, b // 2))
+                add(tri, b, padded=False)
     assert out, f"no plan within {MAX_THREADS} threads for {axis} length {L}"
     return out
 
 
-def choose(axis: str, L: int, column: int | None, tuned: dict) -> tuple[list[int], int, int]:
+def choose(axis: str, L: int, column: int | None,
+           tuned: dict) -> tuple[list[int], int, int, list[int]]:
     c = candidates(axis, L)
     if column is not None:
         return c[column] if column < len(c) else c[0]
     t = tuned.get(axis, {}).get(str(L))
     if t:
-        pick = (t["radices"], t["batch"], t.get("regx", 0))
+        pick = (t["radices"], t["batch"], t.get("regx", 0), t.get("pads", [0, 0]))
         if pick in c:
             return pick
     return c[0]
 
 
-def x_units(xs: list[int], xplans: dict[int, tuple[list[int], int, int]]) -> None:
+def x_units(xs: list[int], xplans: dict) -> None:
     units = [xs[k::X_UNITS] for k in range(X_UNITS)]
     kinds = {
         "fwd": ("const float* X, float* Xm1, const float* lam, int predict, float2* S",
@@ -229,18 +307,18 @@ def x_units(xs: list[int], xplans: dict[int, tuple[list[int], int, int]]) -> Non
                        f"cudaStream_t st, bool* done) {{")
             out.append("  switch (g.nx) {")
             for L in lens:
-                _, P, rx = xplans[L]
+                _, P, rx, (b0, b1) = xplans[L]
                 c = call.replace("PP", str(P))
                 out.append(f"    case {L}:")
                 out.append("      *done = true;")
-                out.append(f"      return {go}<StaticRunner<SPX{L}, {P}, false, false, {rx}>>("
-                           f"{c}, splan_threads<SPX{L}, {P}>(), st);")
+                out.append(f"      return {go}<StaticRunner<SPX{L}, {P}, false, false, {rx}, {b0}, "
+                           f"{b1}>>({c}, splan_threads<SPX{L}, {P}>(), st);")
             out += ["    default:", "      return 0;", "  }", "}", ""]
         out += ["}  // namespace cdx", ""]
         (HERE / "csrc" / f"decon_x_gen_{k}.cu").write_text("\n".join(out))
 
 
-def generate(column: int | None = None) -> dict[str, dict[int, tuple[list[int], int, int]]]:
+def generate(column: int | None = None) -> dict:
     """Write the generated sources; returns the chosen plans per axis."""
     tuned = json.loads(TUNED.read_text()) if column is None and TUNED.exists() else {}
     lens = lengths()
@@ -260,15 +338,16 @@ def generate(column: int | None = None) -> dict[str, dict[int, tuple[list[int], 
     def block(name, items):
         return [f"#define {name}(F) \\"] + [f"  F({i}) \\" for i in items] + [""]
 
-    lines += block("CDX_GEN_SPLANS", [f"{L}, {', '.join(map(str, r))}"
-                                      for L, (r, _, _) in plans["y"].items()])
-    lines += block("CDX_GEN_Z_SPLANS", [f"{L}, {', '.join(map(str, r))}"
-                                        for L, (r, _, _) in plans["z"].items()])
-    lines += block("CDX_GEN_X_SPLANS", [f"{L}, {', '.join(map(str, r))}"
-                                        for L, (r, _, _) in plans["x"].items()])
-    lines += block("CDX_GEN_X_PAIRS", [f"{L}, {P}" for L, (_, P, _) in plans["x"].items()])
-    lines += block("CDX_GEN_Y_PLANS", [f"{L}, {V}, {rx}" for L, (_, V, rx) in plans["y"].items()])
-    lines += block("CDX_GEN_Z_PLANS", [f"{L}, {W}, {rx}" for L, (_, W, rx) in plans["z"].items()])
+    lines += block("CDX_GEN_SPLANS", [f"{L}, {', '.join(map(str, c[0]))}"
+                                      for L, c in plans["y"].items()])
+    lines += block("CDX_GEN_Z_SPLANS", [f"{L}, {', '.join(map(str, c[0]))}"
+                                        for L, c in plans["z"].items()])
+    lines += block("CDX_GEN_X_SPLANS", [f"{L}, {', '.join(map(str, c[0]))}"
+                                        for L, c in plans["x"].items()])
+    lines += block("CDX_GEN_X_PAIRS", [f"{L}, {c[1]}" for L, c in plans["x"].items()])
+    lines += block("CDX_GEN_Y_PLANS", [f"{L}, {c[1]}, {c[2]}, {c[3][0]}, {c[3][1]}"
+                                       for L, c in plans["y"].items()])
+    lines += block("CDX_GEN_Z_PLANS", [f"{L}, {c[1]}, {c[2]}" for L, c in plans["z"].items()])
     OUT.write_text("\n".join(lines) + "\n")
     x_units(lens["x"], plans["x"])
     return plans

@@ -15,6 +15,7 @@ import math
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -31,32 +32,37 @@ def test_candidates_are_valid_plans():
         for L in ls:
             c = G.candidates(axis, L)
             assert c, (axis, L)
-            for rad, batch, regx in c:
+            for rad, batch, regx, pads in c:
                 assert regx in (0, G.REGX)
+                assert all(b in G.PAD_CHOICES for b in pads)
+                assert pads == [0, 0] or (len(rad) == 3 and axis != "z")
                 assert math.prod(rad) == L and max(rad) <= 32 and min(rad) >= 2
                 assert batch >= 1 and G.threads(L, rad, batch) <= G.MAX_THREADS
                 if axis == "x":
                     assert G.x_fits(L, rad, batch)
-            assert len({(tuple(r), b, x) for r, b, x in c}) == len(c)
+            assert len({(tuple(r), b, x, tuple(p)) for r, b, x, p in c}) == len(c)
             assert len(c) <= G.N_COLUMNS
 
 
 def test_candidate_zero_is_the_heuristic():
     for L in G.lengths()["x"]:
-        assert G.candidates("x", L)[0] == (G.radices3(L), G.x_pairs(L), 0)
+        r = G.radices3(L)
+        assert G.candidates("x", L)[0] == (r, G.x_pairs(L), 0, G.smem_pads(L, r, G.x_pairs(L)))
         r = G.candidates("x", L)[0][0]
         assert r == sorted(r, reverse=True)
     for L in G.lengths()["y"]:
-        assert G.candidates("y", L)[0] == (G.radices(L), max(1, 2048 // L), 0)
+        r, V = G.radices(L), max(1, 2048 // L)
+        assert G.candidates("y", L)[0] == (r, V, 0, G.smem_pads(L, r, V))
     for L in G.lengths()["z"]:
-        assert G.candidates("z", L)[0] == (G.radices(L), G.Z_COLS, 0)
+        assert G.candidates("z", L)[0] == (G.radices(L), G.Z_COLS, 0, [0, 0])
 
 
 def test_choose_follows_a_tuned_table_only_for_known_candidates():
     L = 600
     c = G.candidates("x", L)
     assert len(c) > 1
-    tuned = {"x": {"600": {"radices": c[1][0], "batch": c[1][1], "regx": c[1][2]}}}
+    tuned = {"x": {"600": {"radices": c[1][0], "batch": c[1][1], "regx": c[1][2],
+                           "pads": c[1][3]}}}
     assert G.choose("x", L, None, tuned) == c[1]
     bogus = {"x": {"600": {"radices": [600], "batch": 1}}}
     assert G.choose("x", L, None, bogus) == c[0]
@@ -76,6 +82,22 @@ def test_committed_sources_match_the_generator(tmp_path, monkeypatch):
         [f"decon_x_gen_{k}.cu" for k in range(G.X_UNITS)]
     for n in names:
         assert (tmp_path / "csrc" / n).read_text() == (PKG / "csrc" / n).read_text(), n
+
+
+def test_bank_model_counts_known_patterns():
+    # 16 threads at stride 10 float2s: two threads per bank pair -> 2
+    # wavefronts per half-warp; stride 1 -> 1
+    a = np.arange(32) * 10
+    assert G._wavefronts64(a.reshape(1, 32)) == 4
+    assert G._wavefronts64(np.arange(32).reshape(1, 32)) == 2
+    assert G._wavefronts64(np.full((1, 32), -1)) == 0
+    # the padded layout of 1008 = 12*12*7 after its first stage halves the
+    # modelled conflicts of the natural one
+    nat = G.boundary_wavefronts(1008, [12, 12, 7], 4, 0, 0)
+    pad = G.boundary_wavefronts(1008, [12, 12, 7], 4, 0, 48)
+    assert pad < 0.5 * nat
+    assert G.smem_pads(1008, [12, 12, 7], 4)[0] != 0
+    assert G.smem_pads(600, [24, 25], 4) == [0, 0]
 
 
 def test_probe_shapes_cover_every_length():
@@ -100,7 +122,7 @@ def test_select_keeps_candidate_zero_within_the_margin():
     sel = T.select(cols, G.candidates, 0.02)
     assert sel["x"]["600"]["candidate"] == 1
     got = sel["x"]["600"]
-    assert (got["radices"], got["batch"], got["regx"]) == G.candidates("x", 600)[1]
+    assert (got["radices"], got["batch"], got["regx"], got["pads"]) == G.candidates("x", 600)[1]
     assert sel["y"]["320"]["candidate"] == 0
     assert sel["z"]["120"]["candidate"] == 0
     json.dumps(sel)
