@@ -21,16 +21,16 @@ int xgen_fwd_0(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX378, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX378, 4>(), st);
     case 490:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX490, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX490, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX490, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX490, 4>(), st);
     case 640:
       *done = true;
       return x_fwd_go<StaticRunner<SPX640, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX640, 2>(), st);
     case 800:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX800, 4, false, false, 0, 0, 96>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX800, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX800, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX800, 2>(), st);
     case 1000:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX1000, 4, false, false, 0, 0, 96>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX1000, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX1000, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX1000, 2>(), st);
     default:
       return 0;
   }
@@ -52,16 +52,16 @@ int xgen_ratio_0(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX378, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX378, 4>(), st);
     case 490:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX490, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX490, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX490, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX490, 4>(), st);
     case 640:
       *done = true;
       return x_ratio_go<StaticRunner<SPX640, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX640, 2>(), st);
     case 800:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX800, 4, false, false, 0, 0, 96>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX800, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX800, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX800, 2>(), st);
     case 1000:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX1000, 4, false, false, 0, 0, 96>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX1000, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX1000, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX1000, 2>(), st);
     default:
       return 0;
   }
@@ -83,16 +83,16 @@ int xgen_update_0(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX378, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX378, 4>(), st);
     case 490:
       *done = true;
-      return x_update_go<StaticRunner<SPX490, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX490, 8>(), st);
+      return x_update_go<StaticRunner<SPX490, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX490, 4>(), st);
     case 640:
       *done = true;
       return x_update_go<StaticRunner<SPX640, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX640, 2>(), st);
     case 800:
       *done = true;
-      return x_update_go<StaticRunner<SPX800, 4, false, false, 0, 0, 96>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX800, 4>(), st);
+      return x_update_go<StaticRunner<SPX800, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX800, 2>(), st);
     case 1000:
       *done = true;
-      return x_update_go<StaticRunner<SPX1000, 4, false, false, 0, 0, 96>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX1000, 4>(), st);
+      return x_update_go<StaticRunner<SPX1000, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX1000, 2>(), st);
     default:
       return 0;
   }

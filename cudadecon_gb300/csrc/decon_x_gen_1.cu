@@ -15,13 +15,13 @@ int xgen_fwd_1(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX200, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX200, 4>(), st);
     case 288:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX288, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX288, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX288, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX288, 4>(), st);
     case 384:
       *done = true;
       return x_fwd_go<StaticRunner<SPX384, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX384, 8>(), st);
     case 500:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX500, 8, false, false, 0, 0, 16>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX500, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_fwd_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX648, 4>(), st);
@@ -30,7 +30,7 @@ int xgen_fwd_1(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX810, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX810, 2>(), st);
     case 1008:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX1008, 4, false, false, 0, 48, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX1008, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX1008, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX1008, 2>(), st);
     default:
       return 0;
   }
@@ -46,13 +46,13 @@ int xgen_ratio_1(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX200, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX200, 4>(), st);
     case 288:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX288, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX288, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX288, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX288, 4>(), st);
     case 384:
       *done = true;
       return x_ratio_go<StaticRunner<SPX384, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX384, 8>(), st);
     case 500:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX500, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX500, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_ratio_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX648, 4>(), st);
@@ -61,7 +61,7 @@ int xgen_ratio_1(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX810, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX810, 2>(), st);
     case 1008:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX1008, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX1008, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX1008, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX1008, 2>(), st);
     default:
       return 0;
   }
@@ -77,13 +77,13 @@ int xgen_update_1(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX200, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX200, 4>(), st);
     case 288:
       *done = true;
-      return x_update_go<StaticRunner<SPX288, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX288, 8>(), st);
+      return x_update_go<StaticRunner<SPX288, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX288, 4>(), st);
     case 384:
       *done = true;
       return x_update_go<StaticRunner<SPX384, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX384, 8>(), st);
     case 500:
       *done = true;
-      return x_update_go<StaticRunner<SPX500, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX500, 8>(), st);
+      return x_update_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_update_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX648, 4>(), st);
@@ -92,7 +92,7 @@ int xgen_update_1(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX810, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX810, 2>(), st);
     case 1008:
       *done = true;
-      return x_update_go<StaticRunner<SPX1008, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX1008, 4>(), st);
+      return x_update_go<StaticRunner<SPX1008, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX1008, 2>(), st);
     default:
       return 0;
   }

@@ -9,25 +9,25 @@ int xgen_fwd_2(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
   switch (g.nx) {
     case 144:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX144, 8, false, false, 0, 48, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX144, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX144, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX144, 4>(), st);
     case 210:
       *done = true;
       return x_fwd_go<StaticRunner<SPX210, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX210, 8>(), st);
     case 294:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX294, 8, false, false, 0, 0, 16>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX294, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX294, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX294, 4>(), st);
     case 392:
       *done = true;
       return x_fwd_go<StaticRunner<SPX392, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX392, 4>(), st);
     case 504:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX504, 8, false, false, 0, 0, 64>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX504, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX672, 4, false, false, 0, 48, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX672, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX672, 2>(), st);
     case 840:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX840, 4, false, false, 0, 48, 28>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX840, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX840, 2>(), st);
     default:
       return 0;
   }
@@ -37,25 +37,25 @@ int xgen_ratio_2(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
   switch (g.nx) {
     case 144:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX144, 8, false, false, 0, 48, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX144, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX144, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX144, 4>(), st);
     case 210:
       *done = true;
       return x_ratio_go<StaticRunner<SPX210, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX210, 8>(), st);
     case 294:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX294, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX294, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX294, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX294, 4>(), st);
     case 392:
       *done = true;
       return x_ratio_go<StaticRunner<SPX392, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX392, 4>(), st);
     case 504:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX504, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX504, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX672, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX672, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX672, 2>(), st);
     case 840:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX840, 4, false, false, 0, 48, 28>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX840, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX840, 2>(), st);
     default:
       return 0;
   }
@@ -65,25 +65,25 @@ int xgen_update_2(const Geom& g, const FftLen& fx, const float2* S, const float*
   switch (g.nx) {
     case 144:
       *done = true;
-      return x_update_go<StaticRunner<SPX144, 8, false, false, 0, 48, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX144, 8>(), st);
+      return x_update_go<StaticRunner<SPX144, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX144, 4>(), st);
     case 210:
       *done = true;
       return x_update_go<StaticRunner<SPX210, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX210, 8>(), st);
     case 294:
       *done = true;
-      return x_update_go<StaticRunner<SPX294, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX294, 8>(), st);
+      return x_update_go<StaticRunner<SPX294, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX294, 4>(), st);
     case 392:
       *done = true;
       return x_update_go<StaticRunner<SPX392, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX392, 4>(), st);
     case 504:
       *done = true;
-      return x_update_go<StaticRunner<SPX504, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX504, 8>(), st);
+      return x_update_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_update_go<StaticRunner<SPX672, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX672, 4>(), st);
+      return x_update_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX672, 2>(), st);
     case 840:
       *done = true;
-      return x_update_go<StaticRunner<SPX840, 4, false, false, 0, 48, 28>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX840, 4>(), st);
+      return x_update_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX840, 2>(), st);
     default:
       return 0;
   }

@@ -12,10 +12,10 @@ int xgen_fwd_3(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX147, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX147, 8>(), st);
     case 216:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX216, 8, false, false, 0, 48, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX216, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX216, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX216, 4>(), st);
     case 300:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX300, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX300, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
       return x_fwd_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX400, 2>(), st);
@@ -24,7 +24,7 @@ int xgen_fwd_3(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX525, 2>(), st);
     case 675:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX675, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX675, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX675, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX675, 2>(), st);
     case 864:
       *done = true;
       return x_fwd_go<StaticRunner<SPX864, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX864, 2>(), st);
@@ -40,10 +40,10 @@ int xgen_ratio_3(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX147, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX147, 8>(), st);
     case 216:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX216, 8, false, false, 0, 48, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX216, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX216, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX216, 4>(), st);
     case 300:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX300, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX300, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
       return x_ratio_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX400, 2>(), st);
@@ -52,7 +52,7 @@ int xgen_ratio_3(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX525, 2>(), st);
     case 675:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX675, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX675, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX675, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX675, 2>(), st);
     case 864:
       *done = true;
       return x_ratio_go<StaticRunner<SPX864, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX864, 2>(), st);
@@ -68,10 +68,10 @@ int xgen_update_3(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX147, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX147, 8>(), st);
     case 216:
       *done = true;
-      return x_update_go<StaticRunner<SPX216, 8, false, false, 0, 48, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX216, 8>(), st);
+      return x_update_go<StaticRunner<SPX216, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX216, 4>(), st);
     case 300:
       *done = true;
-      return x_update_go<StaticRunner<SPX300, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX300, 8>(), st);
+      return x_update_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
       return x_update_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX400, 2>(), st);
@@ -80,7 +80,7 @@ int xgen_update_3(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX525, 2>(), st);
     case 675:
       *done = true;
-      return x_update_go<StaticRunner<SPX675, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX675, 4>(), st);
+      return x_update_go<StaticRunner<SPX675, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX675, 2>(), st);
     case 864:
       *done = true;
       return x_update_go<StaticRunner<SPX864, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX864, 2>(), st);

@@ -12,13 +12,13 @@ int xgen_fwd_6(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX240, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX240, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX240, 4>(), st);
     case 324:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX324, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX324, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX432, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX432, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
       return x_fwd_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX567, 2>(), st);
@@ -40,13 +40,13 @@ int xgen_ratio_6(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX240, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX240, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX240, 4>(), st);
     case 324:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX324, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX324, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX432, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX432, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
       return x_ratio_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX567, 2>(), st);
@@ -68,13 +68,13 @@ int xgen_update_6(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX162, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX162, 8>(), st);
     case 240:
       *done = true;
-      return x_update_go<StaticRunner<SPX240, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX240, 8>(), st);
+      return x_update_go<StaticRunner<SPX240, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX240, 4>(), st);
     case 324:
       *done = true;
-      return x_update_go<StaticRunner<SPX324, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX324, 8>(), st);
+      return x_update_go<StaticRunner<SPX324, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX324, 4>(), st);
     case 432:
       *done = true;
-      return x_update_go<StaticRunner<SPX432, 8, false, false, 0, 0, 64>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX432, 8>(), st);
+      return x_update_go<StaticRunner<SPX432, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX432, 4>(), st);
     case 567:
       *done = true;
       return x_update_go<StaticRunner<SPX567, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX567, 2>(), st);

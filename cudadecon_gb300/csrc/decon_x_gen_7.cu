@@ -21,7 +21,7 @@ int xgen_fwd_7(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX441, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX576, 4, false, false, 0, 0, 64>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX576, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX576, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_fwd_go<StaticRunner<SPX729, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX729, 4>(), st);
@@ -49,7 +49,7 @@ int xgen_ratio_7(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX441, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX576, 4, false, false, 0, 0, 64>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX576, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX576, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_ratio_go<StaticRunner<SPX729, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX729, 4>(), st);
@@ -77,7 +77,7 @@ int xgen_update_7(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX441, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX441, 4>(), st);
     case 576:
       *done = true;
-      return x_update_go<StaticRunner<SPX576, 4, false, false, 0, 0, 64>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX576, 4>(), st);
+      return x_update_go<StaticRunner<SPX576, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX576, 2>(), st);
     case 729:
       *done = true;
       return x_update_go<StaticRunner<SPX729, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX729, 4>(), st);

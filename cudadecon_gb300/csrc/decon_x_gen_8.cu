@@ -15,19 +15,19 @@ int xgen_fwd_8(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX245, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX245, 8>(), st);
     case 343:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX343, 8, false, false, 0, 0, 16>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX343, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
       return x_fwd_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX448, 8>(), st);
     case 588:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX588, 4, false, false, 0, 48, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX588, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX588, 4>(), st);
     case 735:
       *done = true;
       return x_fwd_go<StaticRunner<SPX735, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX735, 2>(), st);
     case 945:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX945, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX945, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX945, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX945, 2>(), st);
     default:
       return 0;
   }
@@ -43,19 +43,19 @@ int xgen_ratio_8(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX245, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX245, 8>(), st);
     case 343:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX343, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX343, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
       return x_ratio_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX448, 8>(), st);
     case 588:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX588, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX588, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX588, 4>(), st);
     case 735:
       *done = true;
       return x_ratio_go<StaticRunner<SPX735, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX735, 2>(), st);
     case 945:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX945, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX945, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX945, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX945, 2>(), st);
     default:
       return 0;
   }
@@ -71,19 +71,19 @@ int xgen_update_8(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX245, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX245, 8>(), st);
     case 343:
       *done = true;
-      return x_update_go<StaticRunner<SPX343, 8, false, false, 0, 0, 16>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX343, 8>(), st);
+      return x_update_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
       return x_update_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX448, 8>(), st);
     case 588:
       *done = true;
-      return x_update_go<StaticRunner<SPX588, 4, false, false, 0, 48, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX588, 4>(), st);
+      return x_update_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX588, 4>(), st);
     case 735:
       *done = true;
       return x_update_go<StaticRunner<SPX735, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX735, 2>(), st);
     case 945:
       *done = true;
-      return x_update_go<StaticRunner<SPX945, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX945, 4>(), st);
+      return x_update_go<StaticRunner<SPX945, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX945, 2>(), st);
     default:
       return 0;
   }

@@ -34,7 +34,7 @@ Padding (x and y plans of three radices): each layout between two stages
 gets one float2 of padding after every B, with B in PAD_CHOICES picked by a
 model of the shared-memory bank conflicts of the stage that writes it and
 the stage that reads it (smem_pads); every candidate carries its model
-padding, and one more candidate is candidate 0 without it.
+padding (mostly none), and one more candidate is candidate 0 without it.
 
 autotune.py times the candidates on the GPU and records the fastest per
 axis and length in tuned_plans.json, which this script then follows.
@@ -60,7 +60,8 @@ TUNED = HERE / "tuned_plans.json"
 X_UNITS = 12
 N_COLUMNS = 8
 REGX = 16
-PAD_CHOICES = (0, 16, 20, 24, 28, 32, 48, 64, 96, 128)
+PAD_CHOICES = (0, 16, 32, 64, 128)
+PAD_MIN_GAIN = 0.5
 
 REGISTERED = {32, 64, 100, 128, 256, 512, 756, 1024, 1620}
 X_RANGE = (128, 1024)
@@ -188,9 +189,13 @@ def boundary_wavefronts(L: int, rad: list[int], V: int, s: int, B: int) -> int:
 
 
 def smem_pads(L: int, rad: list[int], V: int) -> list[int]:
-    """Padding periods of the two layouts between the stages of a
-    three-radix row plan: the fewest modelled wavefronts, 0 (natural) unless
-    a padding saves at least 5%."""
+    """Padding periods (powers of two: the padded index is a shift and an
+    add) of the two layouts between the stages of a three-radix row plan:
+    per boundary the fewest modelled wavefronts, kept where they save a
+    quarter of that boundary's, and none at all unless the plan's two
+    boundaries together lose more than half.  Measured on the GB300: plans
+    whose model dropped below half ran 5-13% faster padded (radix 8 first,
+    B = 16); those between 0.58 and 0.97 ran up to 8% slower."""
     return list(_smem_pads(L, tuple(rad), V))
 
 
@@ -198,12 +203,20 @@ def smem_pads(L: int, rad: list[int], V: int) -> list[int]:
 def _smem_pads(L: int, rad: tuple[int, ...], V: int) -> tuple[int, int]:
     if len(rad) != 3:
         return (0, 0)
-    out = []
+    nat = [boundary_wavefronts(L, list(rad), V, s, 0) for s in range(2)]
+    pads, cost = [], []
     for s in range(2):
-        cost = {B: boundary_wavefronts(L, list(rad), V, s, B) for B in PAD_CHOICES}
-        best = min(cost, key=lambda B: (cost[B], B))
-        out.append(best if cost[best] <= 0.95 * cost[0] else 0)
-    return tuple(out)
+        c = {B: boundary_wavefronts(L, list(rad), V, s, B) for B in PAD_CHOICES}
+        best = min(c, key=lambda B: (c[B], B))
+        if c[best] > 0.75 * nat[s]:
+            best = 0
+        pads.append(best)
+        cost.append(c[best])
+    # the padded index costs instructions of its own: pad only where the
+    # model removes more than half of the two boundaries' wavefronts
+    if sum(cost) > PAD_MIN_GAIN * sum(nat):
+        return (0, 0)
+    return tuple(pads)
 
 
 def candidates(axis: str, L: int) -> list[tuple[list[int], int, int, list[int]]]:
