@@ -15,6 +15,10 @@
   axis (and on the whole volume).
 * camcor chained into deskew + RL + rotate on the device, against the
   reference's camcor kernel followed by the float32 oracle.
+* One length of every kind of tuned plan in use (padded stage layouts, two-
+  or three-radix plans, other batches, radix orders, register budgets; from
+  cudadecon_gb300/tuned_plans.json), through RL against the reference's
+  kernels.
 
 FP64 on the large grids is the torch restatement of the oracle
 (oracle/rl_oracle_torch.py, cuFFT double), pinned to the numpy FP64 oracle in
@@ -22,7 +26,10 @@ tests/test_oracle_cpu.py.  Tolerances: relative L2 <= 1e-5 against the
 reference's float32 kernels, <= 1e-4 against FP64."""
 
 import ctypes
+import json
 import math
+import sys
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -325,4 +332,61 @@ def test_rl_generated_x_plans_vs_reference(cdx, oracle, ref, torch_cuda, tmp_pat
     theirs, _ = ref.rl_iterations(X0, X0, tab, oracle.kscales(st, gx, gy, gz), 8)
     e = rel_l2(mine, theirs)
     print(f"\ngenerated x plan {gz}x{gy}x{gx}, 8 it: rel L2 vs reference {e:.2e}")
+    assert e < 1e-5
+
+
+def _tuned_variants():
+    """(axis, feature, length): one length per kind of tuned plan in use."""
+    pkg = Path(__file__).resolve().parents[1] / "cudadecon_gb300"
+    if str(pkg) not in sys.path:
+        sys.path.insert(0, str(pkg))
+    import gen_plans as G
+    tuned = json.loads(G.TUNED.read_text()) if G.TUNED.exists() else {}
+    lens = G.lengths()
+    picked = {}
+    for axis in "xyz":
+        for L in lens[axis]:
+            rad, b, rx, pads = G.choose(axis, L, None, tuned)
+            c0 = G.candidates(axis, L)[0]
+            feats = []
+            if pads != [0, 0]:
+                feats.append("padded")
+            if len(rad) != len(c0[0]):
+                feats.append(f"{len(rad)} radices")
+            if rx:
+                feats.append("more registers")
+            if b < c0[1]:
+                feats.append("smaller batch")
+            if b > c0[1]:
+                feats.append("larger batch")
+            if len(rad) == len(c0[0]) and rad != c0[0]:
+                feats.append("radix order")
+            for f in feats:
+                picked.setdefault((axis, f), L)
+    return sorted((a, f, L) for (a, f), L in picked.items())
+
+
+@pytest.mark.parametrize("axis,feature,L", _tuned_variants())
+def test_rl_tuned_plan_variants_vs_reference(cdx, oracle, ref, torch_cuda, tmp_path, axis,
+                                             feature, L):
+    """RL through a tuned generated plan on one axis (the other two lengths
+    small) against the reference's kernels + cuFFT, 8 iterations."""
+    shape = {"x": (10, 24, L), "y": (10, L, 128), "z": (L, 24, 128)}[axis]
+    raw = synth.bead_stack(shape, n_beads=40, psf_sigma_xy=1.3, psf_sigma_z=2.5, seed=L)
+    nz, ny, nx = shape
+    tab = synth.gaussian_otf_table(129, 64, 1.3, 2.5)
+    p = tmp_path / "otf.tif"
+    synth.write_otf(p, tab)
+    kw = dict(dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.25)
+    cdx.rl_init(shape, p, **kw)
+    gz, gy, gx = cdx.decon_grid()
+    assert (gz, gy, gx) == shape
+    mine = cdx.rl_decon(raw, background=100.0, n_iters=8)
+    cdx.rl_cleanup()
+    st = oracle.rl_init(nx, ny, nz, kw["dr"], kw["dz"], kw["dr_psf"], kw["dz_psf"], 0.0, 0.0, 0,
+                        False, synth.otf_table_to_image(tab))
+    X0 = oracle.bgsub(raw.astype(np.float32), 100.0)
+    theirs, _ = ref.rl_iterations(X0, X0, tab, oracle.kscales(st, gx, gy, gz), 8)
+    e = rel_l2(mine, theirs)
+    print(f"\ntuned {axis} plan ({feature}) {gz}x{gy}x{gx}, 8 it: rel L2 vs reference {e:.2e}")
     assert e < 1e-5
