@@ -18,7 +18,7 @@ int xgen_fwd_8(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX448, 8>(), st);
+      return x_fwd_go<StaticRunner<SPX448, 4, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX448, 4>(), st);
     case 588:
       *done = true;
       return x_fwd_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX588, 4>(), st);
@@ -46,7 +46,7 @@ int xgen_ratio_8(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX448, 8>(), st);
+      return x_ratio_go<StaticRunner<SPX448, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX448, 4>(), st);
     case 588:
       *done = true;
       return x_ratio_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX588, 4>(), st);
@@ -74,7 +74,7 @@ int xgen_update_8(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX343, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX343, 4>(), st);
     case 448:
       *done = true;
-      return x_update_go<StaticRunner<SPX448, 8, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX448, 8>(), st);
+      return x_update_go<StaticRunner<SPX448, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX448, 4>(), st);
     case 588:
       *done = true;
       return x_update_go<StaticRunner<SPX588, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX588, 4>(), st);
