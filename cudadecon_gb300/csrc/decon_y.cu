@@ -7,7 +7,7 @@ namespace cdx {
 template <bool INV, class Run>
 __global__ void __launch_bounds__(Run::kThreads, Run::template min_blocks<8>())
 k_y_pass(Geom g, FftDev fy, float2* __restrict__ S, int V) {
-  extern __shared__ float2 smem[];
+  extern __shared__ __align__(16) float2 smem[];
   const int ny = g.ny;
   float2* stw = smem;
   const auto io = Run::row_tile(smem + ny, ny);

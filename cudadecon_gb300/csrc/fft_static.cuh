@@ -54,6 +54,13 @@ __host__ __device__ constexpr int splan_threads() {
   return ((t + 31) / 32) * 32;
 }
 
+// Storers that can write two neighbouring elements as one 16-byte store
+// (kPair; st2 with its alignment test) -- see sstage.
+template <class T, class = void>
+struct has_pair : std::false_type {};
+template <class T>
+struct has_pair<T, std::void_t<decltype(T::kPair)>> : std::bool_constant<T::kPair> {};
+
 // One stage: radix Q, span NS.  Thread b owns butterfly b (if b < V*L/Q).
 template <int L, int Q, int NS, bool INV, int V, bool VFAST, bool SYNC_MID, bool SYNC_END, class Ld,
           class St, bool GTW = false>
@@ -87,7 +94,22 @@ __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St
       }
     }
     DftS<Q, INV>::run(x);
-    store_group<Q>(st, v, (j - k) * Q + k, NS, x);
+    if constexpr (!VFAST && NS == 1 && Q % 2 == 0 && has_pair<St>::value) {
+      // first stage of a row plan: butterfly j's outputs land at j*Q + q,
+      // contiguous, and a half-warp's strided float2 stores (stride Q) hit
+      // each bank twice or more for even Q; as 16-byte pairs the stride is
+      // Q/2 float4s, which for Q = 10, 14 or 6 reaches every bank once, and
+      // the stage issues half the stores.  The tile and row pitch are
+      // 16-byte aligned in every kernel that uses it (st.pair_ok checks).
+      if (st.pair_ok()) {
+#pragma unroll
+        for (int q = 0; q < Q; q += 2) st.st2(v, j * Q + q, x[q], x[q + 1]);
+      } else {
+        store_group<Q>(st, v, j * Q, 1, x);
+      }
+    } else {
+      store_group<Q>(st, v, (j - k) * Q + k, NS, x);
+    }
   }
   if (SYNC_END) __syncthreads();
 }
@@ -98,10 +120,19 @@ __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St
 struct NatIO {
   static constexpr bool kSmem = true;
   static constexpr bool kGroup = false;
+  static constexpr bool kPair = true;
   float2* sm;
   int vs;
   __device__ __forceinline__ float2 ld(int v, int e) const { return sm[v * vs + e]; }
   __device__ __forceinline__ void st(int v, int e, float2 x) const { sm[v * vs + e] = x; }
+  // pairs (e, e + 1) with e even are 16-byte aligned when the tile and the
+  // row pitch are
+  __device__ __forceinline__ bool pair_ok() const {
+    return ((reinterpret_cast<unsigned long long>(sm) & 15) | (vs & 1)) == 0;
+  }
+  __device__ __forceinline__ void st2(int v, int e, float2 a, float2 b) const {
+    *reinterpret_cast<float4*>(sm + v * vs + e) = make_float4(a.x, a.y, b.x, b.y);
+  }
 };
 
 // A row tile with one float2 of padding after every B (B = 0: none): the

@@ -31,10 +31,10 @@ between the stages); candidate 0 is the heuristic choice:
          the swapped radices with half the row pairs.
 
 Padding (x and y plans of three radices): each layout between two stages
-gets one float2 of padding after every B, with B in PAD_CHOICES picked by a
-model of the shared-memory bank conflicts of the stage that writes it and
-the stage that reads it (smem_pads); every candidate carries its model
-padding (mostly none), and one more candidate is candidate 0 without it.
+can get one float2 of padding after every B, with B in PAD_CHOICES picked
+by a model of the shared-memory bank conflicts of the stage that writes it
+and the stage that reads it (smem_pads); one candidate per length carries
+the model's padding where the model finds one.
 
 autotune.py times the candidates on the GPU and records the fastest per
 axis and length in tuned_plans.json, which this script then follows.
@@ -61,7 +61,7 @@ X_UNITS = 12
 N_COLUMNS = 8
 REGX = 16
 PAD_CHOICES = (0, 16, 32, 64, 128)
-PAD_MIN_GAIN = 0.5
+PAD_MIN_GAIN = 0.7
 
 REGISTERED = {32, 64, 100, 128, 256, 512, 756, 1024, 1620}
 X_RANGE = (128, 1024)
@@ -162,11 +162,29 @@ def _wavefronts64(addr: np.ndarray) -> int:
     return int(cnt.max(axis=1).sum())
 
 
+def _wavefronts128(addr: np.ndarray) -> int:
+    """Wavefronts of 16-byte accesses: addr (..., 32) float4 indices (-1:
+    inactive); each quarter-warp is one request."""
+    a = addr.reshape(-1, 8)
+    act = np.concatenate([a >= 0] * 4, axis=1)
+    words = np.where(act, np.concatenate([4 * a + i for i in range(4)], axis=1), -1)
+    words.sort(axis=1)
+    uniq = np.ones_like(words, dtype=bool)
+    uniq[:, 1:] = words[:, 1:] != words[:, :-1]
+    uniq &= words >= 0
+    g = np.broadcast_to(np.arange(words.shape[0])[:, None], words.shape)
+    cnt = np.zeros((words.shape[0], 32), dtype=np.int64)
+    np.add.at(cnt, (g[uniq], words[uniq] % 32), 1)
+    return int(cnt.max(axis=1).sum())
+
+
 def boundary_wavefronts(L: int, rad: list[int], V: int, s: int, B: int) -> int:
     """Wavefronts of the stores of stage s and the loads of stage s + 1 of a
     row plan (sstage in fft_static.cuh: thread b owns butterfly j of vector
     v; loads at j + r L/Q, stores at (j - k) Q + k + r Ns with k = j mod
-    Ns) through the layout padded every B float2s."""
+    Ns) through the layout padded every B float2s.  The first stage's stores
+    into the natural layout (B = 0) go out as 16-byte pairs when its radix is
+    even (sstage's pair path)."""
     T = threads(L, rad, V)
     b = np.arange(T)
     ns = int(np.prod(rad[:s])) if s else 1
@@ -174,6 +192,12 @@ def boundary_wavefronts(L: int, rad: list[int], V: int, s: int, B: int) -> int:
     for kind, Q, nsk in (("st", rad[s], ns), ("ld", rad[s + 1], ns * rad[s])):
         LR = L // Q
         v, j = np.divmod(b, LR)
+        if kind == "st" and nsk == 1 and Q % 2 == 0 and B == 0:
+            r2 = np.arange(0, Q, 2)[:, None]
+            t = (v[None, :] * L + j[None, :] * Q + r2) // 2
+            t = np.where(b[None, :] < V * LR, t, -1)
+            tot += _wavefronts128(t.reshape(len(r2), -1, 32))
+            continue
         r = np.arange(Q)[:, None]
         if kind == "ld":
             e = j[None, :] + r * LR
@@ -193,9 +217,13 @@ def smem_pads(L: int, rad: list[int], V: int) -> list[int]:
     add) of the two layouts between the stages of a three-radix row plan:
     per boundary the fewest modelled wavefronts, kept where they save a
     quarter of that boundary's, and none at all unless the plan's two
-    boundaries together lose more than half.  Measured on the GB300: plans
-    whose model dropped below half ran 5-13% faster padded (radix 8 first,
-    B = 16); those between 0.58 and 0.97 ran up to 8% slower."""
+    boundaries together drop below PAD_MIN_GAIN of the natural layout's.
+    Measured on the GB300 against float2 stores in the natural layout:
+    plans whose model dropped below half ran 5-13% faster padded (radix 8
+    first, B = 16); those between 0.58 and 0.97 ran up to 8% slower.  The
+    first stage now stores 16-byte pairs into the natural layout, which
+    removes most of what the padding did, so the padded plan is one
+    candidate among the others for the tuner to measure."""
     return list(_smem_pads(L, tuple(rad), V))
 
 
@@ -213,7 +241,7 @@ def _smem_pads(L: int, rad: tuple[int, ...], V: int) -> tuple[int, int]:
         pads.append(best)
         cost.append(c[best])
     # the padded index costs instructions of its own: pad only where the
-    # model removes more than half of the two boundaries' wavefronts
+    # model removes more than PAD_MIN_GAIN of the two boundaries' wavefronts
     if sum(cost) > PAD_MIN_GAIN * sum(nat):
         return (0, 0)
     return tuple(pads)
@@ -224,13 +252,15 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int, list[int]]]
     candidate 0 first."""
     out: list[tuple[list[int], int, int, list[int]]] = []
 
-    def add(rad, b, rx=0, padded=True):
+    def add(rad, b, rx=0, padded=False):
         rad = list(rad)
         if axis == "x" and not x_fits(L, rad, b):
             return
         if axis != "x" and threads(L, rad, b) > MAX_THREADS:
             return
         pads = smem_pads(L, rad, b) if padded and axis != "z" else [0, 0]
+        if padded and pads == [0, 0]:
+            return
         c = (rad, b, rx, pads)
         if c not in out:
             out.append(c)
@@ -247,7 +277,7 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int, list[int]]]
         add(base, P, REGX)
         add(base, max(1, P // 4))
         add(swapped, max(1, P // 2))
-        add(base, P, padded=False)
+        add(base, max(1, P // 2), padded=True)
     else:
         base = radices(L)
         b = max(1, 2048 // L) if axis == "y" else Z_COLS
@@ -264,7 +294,7 @@ def candidates(axis: str, L: int) -> list[tuple[list[int], int, int, list[int]]]
             if tri:
                 add(tri, b)
                 add(tri, max(1, b // 2))
-                add(tri, b, padded=False)
+                add(tri, b, padded=True)
     assert out, f"no plan within {MAX_THREADS} threads for {axis} length {L}"
     return out
 
