@@ -9,7 +9,7 @@ int xgen_fwd_10(const Geom& g, const FftLen& fx, const float* X, float* Xm1, con
   switch (g.nx) {
     case 189:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX189, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX189, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX189, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX189, 8>(), st);
     case 252:
       *done = true;
       return x_fwd_go<StaticRunner<SPX252, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX252, 8>(), st);
@@ -24,7 +24,7 @@ int xgen_fwd_10(const Geom& g, const FftLen& fx, const float* X, float* Xm1, con
       return x_fwd_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX625, 2>(), st);
     case 768:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX768, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX768, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX768, 2>(), st);
     case 972:
       *done = true;
       return x_fwd_go<StaticRunner<SPX972, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX972, 2>(), st);
@@ -37,7 +37,7 @@ int xgen_ratio_10(const Geom& g, const FftLen& fx, float2* S, const float* raw, 
   switch (g.nx) {
     case 189:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX189, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX189, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX189, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX189, 8>(), st);
     case 252:
       *done = true;
       return x_ratio_go<StaticRunner<SPX252, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX252, 8>(), st);
@@ -52,7 +52,7 @@ int xgen_ratio_10(const Geom& g, const FftLen& fx, float2* S, const float* raw, 
       return x_ratio_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX625, 2>(), st);
     case 768:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX768, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX768, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX768, 2>(), st);
     case 972:
       *done = true;
       return x_ratio_go<StaticRunner<SPX972, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX972, 2>(), st);
@@ -65,7 +65,7 @@ int xgen_update_10(const Geom& g, const FftLen& fx, const float2* S, const float
   switch (g.nx) {
     case 189:
       *done = true;
-      return x_update_go<StaticRunner<SPX189, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX189, 4>(), st);
+      return x_update_go<StaticRunner<SPX189, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX189, 8>(), st);
     case 252:
       *done = true;
       return x_update_go<StaticRunner<SPX252, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX252, 8>(), st);
@@ -80,7 +80,7 @@ int xgen_update_10(const Geom& g, const FftLen& fx, const float2* S, const float
       return x_update_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX625, 2>(), st);
     case 768:
       *done = true;
-      return x_update_go<StaticRunner<SPX768, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX768, 4>(), st);
+      return x_update_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX768, 2>(), st);
     case 972:
       *done = true;
       return x_update_go<StaticRunner<SPX972, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX972, 2>(), st);

@@ -24,7 +24,7 @@ int xgen_fwd_11(const Geom& g, const FftLen& fx, const float* X, float* Xm1, con
       return x_fwd_go<StaticRunner<SPX630, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX630, 4>(), st);
     case 784:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX784, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX784, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX784, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX784, 2>(), st);
     case 980:
       *done = true;
       return x_fwd_go<StaticRunner<SPX980, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX980, 2>(), st);
@@ -52,7 +52,7 @@ int xgen_ratio_11(const Geom& g, const FftLen& fx, float2* S, const float* raw, 
       return x_ratio_go<StaticRunner<SPX630, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX630, 4>(), st);
     case 784:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX784, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX784, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX784, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX784, 2>(), st);
     case 980:
       *done = true;
       return x_ratio_go<StaticRunner<SPX980, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX980, 2>(), st);
@@ -80,7 +80,7 @@ int xgen_update_11(const Geom& g, const FftLen& fx, const float2* S, const float
       return x_update_go<StaticRunner<SPX630, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX630, 4>(), st);
     case 784:
       *done = true;
-      return x_update_go<StaticRunner<SPX784, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX784, 4>(), st);
+      return x_update_go<StaticRunner<SPX784, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX784, 2>(), st);
     case 980:
       *done = true;
       return x_update_go<StaticRunner<SPX980, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX980, 2>(), st);

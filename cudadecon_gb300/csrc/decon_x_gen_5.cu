@@ -12,7 +12,7 @@ int xgen_fwd_5(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX225, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX225, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
       return x_fwd_go<StaticRunner<SPX320, 4, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX320, 4>(), st);
@@ -21,7 +21,7 @@ int xgen_fwd_5(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX420, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX420, 4>(), st);
     case 560:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX560, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX560, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX560, 4>(), st);
     case 700:
       *done = true;
       return x_fwd_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX700, 4>(), st);
@@ -40,7 +40,7 @@ int xgen_ratio_5(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX225, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX225, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
       return x_ratio_go<StaticRunner<SPX320, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX320, 4>(), st);
@@ -49,7 +49,7 @@ int xgen_ratio_5(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX420, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX420, 4>(), st);
     case 560:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX560, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX560, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX560, 4>(), st);
     case 700:
       *done = true;
       return x_ratio_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX700, 4>(), st);
@@ -68,7 +68,7 @@ int xgen_update_5(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX160, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX160, 4>(), st);
     case 225:
       *done = true;
-      return x_update_go<StaticRunner<SPX225, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX225, 4>(), st);
+      return x_update_go<StaticRunner<SPX225, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX225, 2>(), st);
     case 320:
       *done = true;
       return x_update_go<StaticRunner<SPX320, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX320, 4>(), st);
@@ -77,7 +77,7 @@ int xgen_update_5(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX420, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX420, 4>(), st);
     case 560:
       *done = true;
-      return x_update_go<StaticRunner<SPX560, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX560, 2>(), st);
+      return x_update_go<StaticRunner<SPX560, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX560, 4>(), st);
     case 700:
       *done = true;
       return x_update_go<StaticRunner<SPX700, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX700, 4>(), st);
