@@ -868,6 +868,7 @@ def run_gb300(args):
                        "decon_voxels": vox_iters // BATCH["iterations"],
                        "iterations": BATCH["iterations"], "form": "plain FP32",
                        "parallelism": f"replicas x{world}",
+                       "graph_streams": dict(zip(("device", "host"), cdx.batch_streams())),
                        "l2_policy": "working set ~10 GB > 129 MB L2 (no flush needed)"},
             "forms": {"plain": {"value": value, "ms_per_step": ms},
                       "mixed": {"value": value_mixed, "ms_per_step": ms_mixed,

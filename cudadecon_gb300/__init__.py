@@ -136,6 +136,8 @@ def _bind(L) -> None:
         "cdx_RL_batch_device": (c_int, [POINTER(BatchStack), c_int, c_int, c_void_p]),
         "cdx_RL_batch_host": (c_int, [POINTER(BatchStack), c_int, c_int]),
         "cdx_batch_last_launch_count": (c_longlong, []),
+        "cdx_batch_set_streams": (c_int, [c_int, c_int]),
+        "cdx_batch_get_streams": (c_int, [POINTER(c_int), POINTER(c_int)]),
         "cdx_batch_release": (None, []),
     }
     for name, (res, args) in sig.items():
@@ -368,6 +370,21 @@ def rl_batch(stacks, n_iters=10, stream=None):
     if ok != 1:
         _err("cdx_RL_batch_device")
     return outs
+
+
+def batch_streams(device=None, host=None):
+    """Get, or set and get, the streams the batch spreads its stacks over
+    (cdx_batch_set_streams): returns (device_streams, host_streams)."""
+    L = lib()
+    d, h = c_int(0), c_int(0)
+    L.cdx_batch_get_streams(ctypes.byref(d), ctypes.byref(h))
+    if device is not None or host is not None:
+        nd = d.value if device is None else int(device)
+        nh = h.value if host is None else int(host)
+        if L.cdx_batch_set_streams(nd, nh) != 1:
+            raise ValueError(L.cdx_last_error().decode())
+        L.cdx_batch_get_streams(ctypes.byref(d), ctypes.byref(h))
+    return d.value, h.value
 
 
 def rl_batch_host(stacks, n_iters=10, results=None):

@@ -316,6 +316,14 @@ int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* 
  * results are in the host buffers, 0 on failure (extension). */
 int cdx_RL_batch_host(const cdx_batch_stack* stacks, int n, int nIters);
 
+/* Streams the batch's per-stack chains are spread over: device_streams for
+ * cdx_RL_batch_device (default 2), host_streams for cdx_RL_batch_host
+ * (default 4), each in [1, 16].  The next batch call recaptures its graph
+ * when its count changed.  Results do not depend on the counts.  Returns 1,
+ * or 0 for a count out of range (extension). */
+int cdx_batch_set_streams(int device_streams, int host_streams);
+int cdx_batch_get_streams(int* device_streams, int* host_streams);
+
 /* Number of kernel launches (graph nodes included) of the last batch call. */
 long long cdx_batch_last_launch_count(void);
 

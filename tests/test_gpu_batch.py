@@ -120,3 +120,34 @@ def test_batch_host_rejects_pageable_buffers(cdx, torch_cuda):
     host = [dict(st[0], raw=st[0]["raw"].cpu())]  # not pinned
     with pytest.raises(cdx.CudaDeconError, match="page-locked"):
         cdx.rl_batch_host(host, n_iters=2)
+
+
+def test_batch_results_do_not_depend_on_the_stream_counts(cdx, torch_cuda):
+    """The stacks' chains spread over 1, 3 or 16 streams (device batch) and
+    1 or 5 (host batch) give the default counts' results bit for bit; the
+    graph is captured again when a count changes; out-of-range counts are
+    refused."""
+    torch = torch_cuda
+    st = _stacks(torch)
+    default = cdx.batch_streams()
+    assert default == (2, 4)
+    ref = [o.cpu().numpy() for o in cdx.rl_batch(st, n_iters=4)]
+    host = [dict(d, raw=d["raw"].cpu().pin_memory()) for d in st]
+    try:
+        for k in (1, 3, 16):
+            assert cdx.batch_streams(device=k) == (k, 4)
+            outs = cdx.rl_batch(st, n_iters=4)
+            torch.cuda.synchronize()
+            for o, r in zip(outs, ref):
+                assert np.array_equal(o.cpu().numpy(), r)
+        for k in (1, 5):
+            assert cdx.batch_streams(host=k)[1] == k
+            for o, r in zip(cdx.rl_batch_host(host, n_iters=4), ref):
+                assert np.array_equal(o.numpy(), r)
+        L = cdx.lib()
+        assert L.cdx_batch_set_streams(0, 4) == 0
+        assert L.cdx_batch_set_streams(2, 17) == 0
+    finally:
+        cdx.batch_streams(device=default[0], host=default[1])
+        cdx.lib().cdx_batch_release()
+    assert cdx.batch_streams() == default
