@@ -708,15 +708,16 @@ static int init_session(Session& s, int nx, int ny, int nz, float dr, float dz, 
 // calls.  The iterations of all stacks are captured once into a CUDA graph:
 // the stacks, largest first, each go to the least-loaded of K streams forked
 // from the origin stream, so the graph holds K independent chains of about
-// equal work and small stacks run concurrently.  K is 2 for the device batch
-// and 4 for the host batch by default (cdx_batch_set_streams): on the
-// 64-stack uneven batch, device-resident, 1, 2, 3, 4, 6, 8 and 16 streams
-// gave 42.7, 44.6, 43.9, 42.6, 40.2, 39.9 and 39.9 G voxel-iter/s (more
-// concurrent stacks share the L2 that holds a stack's spectrum between its
-// passes), and with the host transfers in the graph 4 streams overlapped
-// them best (40.1 G against 35.1 G with 2).
+// equal work and small stacks run concurrently.  K is 2 by default
+// (cdx_batch_set_streams): on the 64-stack uneven batch, device-resident,
+// 1, 2, 3, 4, 6, 8 and 16 streams gave 42.7, 44.6, 43.9, 42.6, 40.2, 39.9 and
+// 39.9 G voxel-iter/s (more concurrent stacks share the L2 that holds a
+// stack's spectrum between its passes).  The host batch's transfers run on
+// an upload and a download stream of their own, so they overlap the chains
+// whatever K is: 1, 2, 3, 4 and 6 streams gave 42.7, 44.8, 44.0, 42.6 and
+// 39.2 G end to end.
 constexpr int kBatchStreams = 16;
-static int g_batch_streams[2] = {2, 4};  // device batch, host batch
+static int g_batch_streams[2] = {2, 2};  // device batch, host batch
 
 struct BatchStack {
   int nx = 0, ny = 0, nz = 0;  // caller's stack
@@ -759,6 +760,9 @@ struct Batch {
   cudaStream_t fan[kBatchStreams] = {};
   cudaEvent_t ev_in = nullptr, ev_out = nullptr, ev_fork = nullptr;
   cudaEvent_t ev_join[kBatchStreams] = {};
+  // host batch: uploads and downloads run on streams of their own
+  cudaStream_t up = nullptr, dn = nullptr;
+  cudaEvent_t ev_up = nullptr, ev_dn = nullptr, ev_jup = nullptr, ev_jdn = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_iters = -1;
   int graph_form = -1;  // DFT form the graph's kernels were captured with
@@ -790,6 +794,14 @@ struct Batch {
     if (ev_fork) cudaEventDestroy(ev_fork);
     origin = nullptr;
     ev_in = ev_out = ev_fork = nullptr;
+    for (cudaStream_t* q : {&up, &dn}) {
+      if (*q) cudaStreamDestroy(*q);
+      *q = nullptr;
+    }
+    for (cudaEvent_t* ev : {&ev_up, &ev_dn, &ev_jup, &ev_jdn}) {
+      if (*ev) cudaEventDestroy(*ev);
+      *ev = nullptr;
+    }
   }
 };
 static Batch g_b;
@@ -804,6 +816,10 @@ static int batch_streams(Batch& b) {
     CDX_CHECK(cudaStreamCreateWithFlags(&b.fan[i], cudaStreamNonBlocking));
     CDX_CHECK(cudaEventCreateWithFlags(&b.ev_join[i], cudaEventDisableTiming));
   }
+  CDX_CHECK(cudaStreamCreateWithFlags(&b.up, cudaStreamNonBlocking));
+  CDX_CHECK(cudaStreamCreateWithFlags(&b.dn, cudaStreamNonBlocking));
+  for (cudaEvent_t* ev : {&b.ev_up, &b.ev_dn, &b.ev_jup, &b.ev_jdn})
+    CDX_CHECK(cudaEventCreateWithFlags(ev, cudaEventDisableTiming));
   return 0;
 }
 
@@ -858,8 +874,9 @@ static int batch_setup_stack(BatchStack& b, const cdx_batch_stack& d, bool* chan
 }
 
 // Capture the iterations of every stack into b.exec; with host, each
-// stack's chain also uploads and conditions its raw stack first and
-// downloads its result last.
+// stack's chain also conditions its raw stack first, after its upload on
+// the upload stream, and its result is downloaded on the download stream
+// after the chain ends, so the transfers overlap the chains.
 static int batch_capture(Batch& b, int nIters, bool host) {
   b.drop_graph();
   std::vector<int> order(b.st.size());
@@ -874,6 +891,8 @@ static int batch_capture(Batch& b, int nIters, bool host) {
   long long launches = 0;
   cudaError_t e = cudaEventRecord(b.ev_fork, b.origin);
   for (int k = 0; k < K && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b.fan[k], b.ev_fork, 0);
+  if (host && e == cudaSuccess) e = cudaStreamWaitEvent(b.up, b.ev_fork, 0);
+  if (host && e == cudaSuccess) e = cudaStreamWaitEvent(b.dn, b.ev_fork, 0);
   if (e != cudaSuccess) {
     set_cuda_error("batch capture", e);
     rc = e;
@@ -889,10 +908,14 @@ static int batch_capture(Batch& b, int nIters, bool host) {
     load[ks] += (long long)n;
     cudaStream_t s = b.fan[ks];
     if (host) {
-      // the stack's upload and conditioning head its chain
+      // the stack's upload runs on the upload stream (all uploads back to
+      // back, in the order the chains need them); its conditioning heads
+      // its chain once the upload is in
       const size_t nin = (size_t)t.nx * t.ny * t.nz;
       if ((e = cudaMemcpyAsync(t.u16.p, t.h_raw, nin * sizeof(unsigned short),
-                               cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+                               cudaMemcpyHostToDevice, b.up)) != cudaSuccess ||
+          (e = cudaEventRecord(b.ev_up, b.up)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(s, b.ev_up, 0)) != cudaSuccess) {
         set_cuda_error("batch capture", e);
         rc = e;
         break;
@@ -913,10 +936,13 @@ static int batch_capture(Batch& b, int nIters, bool host) {
                       (int)(t.partials.n / 2)};
     rc = rl_loop(t.plan, lb, nIters, s, false, &t.final_x, &launches);
     if (!rc && host) {
-      // and its download ends it (nIters == 0: the conditioned stack)
+      // and its download, on the download stream, follows the chain's end
+      // (nIters == 0: the conditioned stack)
       const float* src = nIters > 0 ? t.final_x : t.Xa.p;
-      if ((e = cudaMemcpyAsync(t.h_result, src, n * sizeof(float), cudaMemcpyDeviceToHost, s)) !=
-          cudaSuccess) {
+      if ((e = cudaEventRecord(b.ev_dn, s)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(b.dn, b.ev_dn, 0)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(t.h_result, src, n * sizeof(float), cudaMemcpyDeviceToHost,
+                               b.dn)) != cudaSuccess) {
         set_cuda_error("batch capture", e);
         rc = e;
       }
@@ -925,6 +951,15 @@ static int batch_capture(Batch& b, int nIters, bool host) {
   for (int k = 0; k < K && !rc; ++k) {
     if ((e = cudaEventRecord(b.ev_join[k], b.fan[k])) != cudaSuccess ||
         (e = cudaStreamWaitEvent(b.origin, b.ev_join[k], 0)) != cudaSuccess) {
+      set_cuda_error("batch capture", e);
+      rc = e;
+    }
+  }
+  if (host && !rc) {
+    if ((e = cudaEventRecord(b.ev_jup, b.up)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(b.origin, b.ev_jup, 0)) != cudaSuccess ||
+        (e = cudaEventRecord(b.ev_jdn, b.dn)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(b.origin, b.ev_jdn, 0)) != cudaSuccess) {
       set_cuda_error("batch capture", e);
       rc = e;
     }

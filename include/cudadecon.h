@@ -309,16 +309,18 @@ int cdx_RL_batch_device(const cdx_batch_stack* stacks, int n, int nIters, void* 
 
 /* cdx_RL_batch_device with the stacks and results in host memory: raw and
  * result of every stack are page-locked host buffers (cudaHostAlloc or
- * cudaHostRegister; pageable memory is rejected).  Each stack's upload,
- * conditioning and download are nodes of its chain in the captured graph,
- * so transfers overlap the other stacks' iterations; the graph is also kept
+ * cudaHostRegister; pageable memory is rejected).  The uploads (in the
+ * order the chains need them) and the downloads (each after its stack's
+ * chain) are nodes of the captured graph on streams of their own, so
+ * transfers overlap the stacks' iterations; the graph is also kept
  * while the host buffers and backgrounds stay the same.  Returns 1 once the
  * results are in the host buffers, 0 on failure (extension). */
 int cdx_RL_batch_host(const cdx_batch_stack* stacks, int n, int nIters);
 
 /* Streams the batch's per-stack chains are spread over: device_streams for
- * cdx_RL_batch_device (default 2), host_streams for cdx_RL_batch_host
- * (default 4), each in [1, 16].  The next batch call recaptures its graph
+ * cdx_RL_batch_device, host_streams for cdx_RL_batch_host (whose uploads
+ * and downloads run on two more streams of their own); default 2 each, each
+ * in [1, 16].  The next batch call recaptures its graph
  * when its count changed.  Results do not depend on the counts.  Returns 1,
  * or 0 for a count out of range (extension). */
 int cdx_batch_set_streams(int device_streams, int host_streams);

@@ -130,12 +130,12 @@ def test_batch_results_do_not_depend_on_the_stream_counts(cdx, torch_cuda):
     torch = torch_cuda
     st = _stacks(torch)
     default = cdx.batch_streams()
-    assert default == (2, 4)
+    assert default == (2, 2)
     ref = [o.cpu().numpy() for o in cdx.rl_batch(st, n_iters=4)]
     host = [dict(d, raw=d["raw"].cpu().pin_memory()) for d in st]
     try:
         for k in (1, 3, 16):
-            assert cdx.batch_streams(device=k) == (k, 4)
+            assert cdx.batch_streams(device=k) == (k, 2)
             outs = cdx.rl_batch(st, n_iters=4)
             torch.cuda.synchronize()
             for o, r in zip(outs, ref):
