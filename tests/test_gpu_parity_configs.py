@@ -6,7 +6,9 @@
   dev_otfinterpolate (src/RLgpuImpl.cu:274-319) through the whole RL loop,
   against the reference's kernels.
 * Six of the 64 uneven stacks of the batched workload (including the longest
-  x), through cdx_RL_batch_device, against the reference's kernels and FP64.
+  x), through cdx_RL_batch_device, against the reference's kernels and FP64;
+  all 64 stacks of the headline batch, as bench.py generates them, against
+  the reference's kernels.
 * The acceleration factors of the library (float-float dot products, lambda
   in double) against the reference's (float products summed in double,
   RLgpuImpl.cu:584-592; lambda on the host, RL-Biggs-Andrews.cpp:297-298).
@@ -210,6 +212,39 @@ def test_batch_subset_of_uneven_stacks_vs_reference_and_fp64(cdx, oracle, ref, t
               f"vs FP64 {e64:.2e}")
         assert e_ref < 1e-5, (i, e_ref)
         assert e64 < 1e-4, (i, e64)
+
+
+def test_batch_all_64_headline_stacks_vs_reference(cdx, oracle, ref, torch_cuda):
+    """Every stack of the headline batch, generated as bench.py generates it
+    (the same seeded draws), through cdx_RL_batch_device with the default
+    graph streams and the tuned plans, against the reference's kernels +
+    cuFFT on the same stack: relative L2 <= 1e-5 for each."""
+    torch = torch_cuda
+    shapes, jit = _batch_shapes()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(BATCH_SEED)
+    stacks = []
+    for i in range(64):
+        lam = 100.0 + 3000.0 * (torch.rand(shapes[i], generator=gen, device="cuda") < 2e-4).float()
+        raw = torch.poisson(lam, generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.uint16)
+        tab = synth.gaussian_otf_table(129, 64, 1.5 * jit[i][0], 4.0 * jit[i][1])
+        stacks.append(dict(raw=raw, otf=tab, dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.3,
+                           background=100.0))
+    outs = cdx.rl_batch(stacks, n_iters=10)
+    torch.cuda.synchronize()
+    cdx.lib().cdx_batch_release()
+    worst = (0.0, None)
+    for i, (d, o) in enumerate(zip(stacks, outs)):
+        gz, gy, gx = cdx.batch_grid(shapes[i])
+        st = oracle.rl_init(shapes[i][2], shapes[i][1], shapes[i][0], 0.104, 0.3, 0.104, 0.3,
+                            0.0, 0.0, 0, False, synth.otf_table_to_image(d["otf"]))
+        X0 = (d["raw"][:gz, :gy, :gx].float() - 100.0).clamp_min_(0.0).cpu().numpy()
+        theirs, _ = ref.rl_iterations(X0, X0, d["otf"], oracle.kscales(st, gx, gy, gz), 10)
+        e = rel_l2(o.cpu().numpy(), theirs)
+        worst = max(worst, (e, (i, shapes[i])))
+        assert e < 1e-5, (i, shapes[i], e)
+    print(f"\n64 headline stacks, 10 it: worst rel L2 vs reference {worst[0]:.2e} (stack "
+          f"{worst[1][0]}, {worst[1][1]})")
 
 
 def test_lambda_sequence_vs_reference_fp64_sums(cdx, oracle, ref, torch_cuda, tmp_path):
