@@ -214,11 +214,12 @@ def test_batch_subset_of_uneven_stacks_vs_reference_and_fp64(cdx, oracle, ref, t
         assert e64 < 1e-4, (i, e64)
 
 
-def test_batch_all_64_headline_stacks_vs_reference(cdx, oracle, ref, torch_cuda):
+def test_batch_all_64_headline_stacks_vs_reference_and_fp64(cdx, oracle, ref, torch_cuda):
     """Every stack of the headline batch, generated as bench.py generates it
     (the same seeded draws), through cdx_RL_batch_device with the default
     graph streams and the tuned plans, against the reference's kernels +
-    cuFFT on the same stack: relative L2 <= 1e-5 for each."""
+    cuFFT on the same stack (relative L2 <= 1e-5 for each) and against FP64
+    (<= 1e-4 for each; the whole batch's error is printed)."""
     torch = torch_cuda
     shapes, jit = _batch_shapes()
     gen = torch.Generator(device="cuda")
@@ -233,18 +234,30 @@ def test_batch_all_64_headline_stacks_vs_reference(cdx, oracle, ref, torch_cuda)
     outs = cdx.rl_batch(stacks, n_iters=10)
     torch.cuda.synchronize()
     cdx.lib().cdx_batch_release()
-    worst = (0.0, None)
+    from oracle import rl_oracle_torch as OT
+    worst, worst64 = (0.0, None), (0.0, None)
+    sq = sq64 = ref2 = 0.0
     for i, (d, o) in enumerate(zip(stacks, outs)):
         gz, gy, gx = cdx.batch_grid(shapes[i])
         st = oracle.rl_init(shapes[i][2], shapes[i][1], shapes[i][0], 0.104, 0.3, 0.104, 0.3,
                             0.0, 0.0, 0, False, synth.otf_table_to_image(d["otf"]))
-        X0 = (d["raw"][:gz, :gy, :gx].float() - 100.0).clamp_min_(0.0).cpu().numpy()
-        theirs, _ = ref.rl_iterations(X0, X0, d["otf"], oracle.kscales(st, gx, gy, gz), 10)
+        X0 = (d["raw"][:gz, :gy, :gx].float() - 100.0).clamp_min_(0.0).contiguous()
+        Xn = X0.cpu().numpy()
+        theirs, _ = ref.rl_iterations(Xn, Xn, d["otf"], oracle.kscales(st, gx, gy, gz), 10)
         e = rel_l2(o.cpu().numpy(), theirs)
         worst = max(worst, (e, (i, shapes[i])))
+        fp64 = OT.rl_iterations(X0, X0, OT.otf_on_grid(st, gx, gy, gz), 10)
+        diff = o.double() - fp64
+        e64 = float(diff.norm() / fp64.norm())
+        worst64 = max(worst64, (e64, (i, shapes[i])))
+        sq64 += float(diff.norm()) ** 2
+        ref2 += float(fp64.norm()) ** 2
+        del fp64, diff
         assert e < 1e-5, (i, shapes[i], e)
+        assert e64 < 1e-4, (i, shapes[i], e64)
     print(f"\n64 headline stacks, 10 it: worst rel L2 vs reference {worst[0]:.2e} (stack "
-          f"{worst[1][0]}, {worst[1][1]})")
+          f"{worst[1][0]}, {worst[1][1]}); vs FP64 worst {worst64[0]:.2e} (stack "
+          f"{worst64[1][0]}), whole batch {math.sqrt(sq64 / ref2):.2e}")
 
 
 def test_lambda_sequence_vs_reference_fp64_sums(cdx, oracle, ref, torch_cuda, tmp_path):
