@@ -249,7 +249,8 @@ def test_batch_all_64_headline_stacks_vs_reference_and_fp64(cdx, oracle, ref, to
         fp64 = OT.rl_iterations(X0, X0, OT.otf_on_grid(st, gx, gy, gz), 10)
         diff = o.double() - fp64
         e64 = float(diff.norm() / fp64.norm())
-        worst64 = max(worst64, (e64, (i, shapes[i])))
+        ref64 = float((torch.from_numpy(theirs).cuda().double() - fp64).norm() / fp64.norm())
+        worst64 = max(worst64, (e64, (i, shapes[i], ref64)))
         sq64 += float(diff.norm()) ** 2
         ref2 += float(fp64.norm()) ** 2
         del fp64, diff
@@ -257,7 +258,8 @@ def test_batch_all_64_headline_stacks_vs_reference_and_fp64(cdx, oracle, ref, to
         assert e64 < 1e-4, (i, shapes[i], e64)
     print(f"\n64 headline stacks, 10 it: worst rel L2 vs reference {worst[0]:.2e} (stack "
           f"{worst[1][0]}, {worst[1][1]}); vs FP64 worst {worst64[0]:.2e} (stack "
-          f"{worst64[1][0]}), whole batch {math.sqrt(sq64 / ref2):.2e}")
+          f"{worst64[1][0]}; the reference's own {worst64[1][2]:.2e}), whole batch "
+          f"{math.sqrt(sq64 / ref2):.2e}")
 
 
 def test_lambda_sequence_vs_reference_fp64_sums(cdx, oracle, ref, torch_cuda, tmp_path):
