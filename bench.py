@@ -808,6 +808,9 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     import cudadecon_gb300 as cdx
     L = cdx.lib()
+    if args.batch_streams:
+        d_s, h_s = (int(v) for v in args.batch_streams.split(","))
+        cdx.batch_streams(device=d_s, host=h_s)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     stacks = batch_inputs(dev)
@@ -918,6 +921,9 @@ def main():
                     help="run one workload alone and print its result (for profiling)")
     ap.add_argument("--zyx", default="100,256,600",
                     help="stack shape z,y,x of --only stack")
+    ap.add_argument("--batch-streams", default=None,
+                    help="DEVICE,HOST graph streams of the batch (cdx_batch_set_streams; "
+                         "default: the library's, 2,2)")
     args = ap.parse_args()
     if args.only:
         return run_only(args)
