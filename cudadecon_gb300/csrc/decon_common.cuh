@@ -346,6 +346,65 @@ struct PackedSpecLoad {
   }
 };
 
+// PackedSpecLoad for a compile-time row length NX (the x kernels of the
+// compile-time plans).  The first stage of those plans reads element
+// e = R*LR + j of vector v with R and LR compile-time and 0 <= j < LR
+// (ld_at): whether e lies in the lower half (k = e) or the upper (k = NX -
+// e), and whether it can be the DC or Nyquist bin, is then known at compile
+// time for every R but the one whose range straddles NX/2 + 1.  Same values
+// as PackedSpecLoad, without its per-element selects.
+template <int NX>
+struct PackedSpecLoadS {
+  static constexpr bool kSmem = true;
+  static constexpr bool kGroup = false;
+  static constexpr bool kLdAt = true;
+  static constexpr int NXH = NX / 2 + 1;
+  const float4* stg;
+  int npairs;  // pairs with rows inside the volume
+  __device__ __forceinline__ static float2 lo_val(float4 w) {
+    return make_float2(w.x - w.w, w.y + w.z);
+  }
+  __device__ __forceinline__ static float2 hi_val(float4 w) {
+    return make_float2(w.x + w.w, w.z - w.y);
+  }
+  __device__ __forceinline__ float2 ld(int v, int e) const {
+    if (v >= npairs) return make_float2(0.f, 0.f);
+    const bool lo = e < NXH;
+    const int k = lo ? e : NX - e;
+    float4 w = stg[v * NXH + k];
+    if (k == 0 || 2 * k == NX) {
+      w.y = 0.f;
+      w.w = 0.f;
+    }
+    return lo ? lo_val(w) : hi_val(w);
+  }
+  template <int R, int LR>
+  __device__ __forceinline__ float2 ld_at(int v, int j) const {
+    constexpr int e0 = R * LR;  // e = e0 + j, 0 <= j < LR
+    if constexpr (e0 + LR <= NXH) {
+      if (v >= npairs) return make_float2(0.f, 0.f);
+      const int k = e0 + j;
+      float4 w = stg[v * NXH + k];
+      // the DC bin (e = 0) and, for even NX, the Nyquist bin (e = NX/2)
+      constexpr bool has_dc = e0 == 0;
+      constexpr bool has_nyq = NX % 2 == 0 && e0 <= NX / 2 && NX / 2 < e0 + LR;
+      if constexpr (has_dc || has_nyq) {
+        if ((has_dc && j == 0) || (has_nyq && k == NX / 2)) {
+          w.y = 0.f;
+          w.w = 0.f;
+        }
+      }
+      return lo_val(w);
+    } else if constexpr (e0 >= NXH) {
+      // upper half: k = NX - e in [1, NX/2), neither DC nor Nyquist
+      if (v >= npairs) return make_float2(0.f, 0.f);
+      return hi_val(stg[v * NXH + (NX - e0 - j)]);
+    } else {
+      return ld(v, e0 + j);
+    }
+  }
+};
+
 // Rows r0 + v of the spectrum (one (kx, z) row of length ny each).
 struct SpecRowIO {
   static constexpr bool kSmem = false;

@@ -86,9 +86,14 @@ k_x_inv_ratio_fwd(Geom g, FftDev fx, float2* __restrict__ S, const float* __rest
   cp_async_commit();
   cp_async_wait_all();
   __syncthreads();
-  const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
   const RatioStore<typename Run::Tile> rs{io, raws, y0, g.ny, nx, eps};
-  Run::template run<true>(fx, P, 1.f, false, stw, io, ld, rs);
+  if constexpr (Run::kStatic) {
+    const PackedSpecLoadS<Run::SPlanT::kL> ld{stg, (nr + 1) / 2};
+    Run::template run<true>(fx, P, 1.f, false, stw, io, ld, rs);
+  } else {
+    const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
+    Run::template run<true>(fx, P, 1.f, false, stw, io, ld, rs);
+  }
   Run::template run<false>(fx, P, 1.f, false, stw, io, io, io);
   store_half_spectra<Run::kV>(g, io, P, z, y0, S);
 }
@@ -185,10 +190,15 @@ k_x_inv_update(Geom g, FftDev fx, const float2* __restrict__ S, const float* Y, 
   cp_async_commit();
   cp_async_wait_all();
   __syncthreads();
-  const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   const UpdateStore us{Ys, Gs, Xout, G, dots, (long long)z * g.ny * nx, y0, g.ny, nx, acc};
-  Run::template run<true>(fx, P, 1.f, false, stw, io, ld, us);
+  if constexpr (Run::kStatic) {
+    const PackedSpecLoadS<Run::SPlanT::kL> ld{stg, (nr + 1) / 2};
+    Run::template run<true>(fx, P, 1.f, false, stw, io, ld, us);
+  } else {
+    const PackedSpecLoad ld{stg, g.nxh, nx, (nr + 1) / 2};
+    Run::template run<true>(fx, P, 1.f, false, stw, io, ld, us);
+  }
   if (!dots) return;
   const float4 sum = block_sum2_ff(acc[0], acc[1], acc[2], acc[3], red);
   if (threadIdx.x == 0) partials[blockIdx.y * gridDim.x + blockIdx.x] = sum;

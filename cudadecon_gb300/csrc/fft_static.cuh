@@ -54,6 +54,13 @@ __host__ __device__ constexpr int splan_threads() {
   return ((t + 31) / 32) * 32;
 }
 
+// Loaders that read element R*LR + j (0 <= j < LR) of a vector through
+// ld_at<R, LR>(v, j), with R and LR compile-time (kLdAt) -- see sstage.
+template <class T, class = void>
+struct has_ld_at : std::false_type {};
+template <class T>
+struct has_ld_at<T, std::void_t<decltype(T::kLdAt)>> : std::bool_constant<T::kLdAt> {};
+
 // Storers that can write two neighbouring elements as one 16-byte store
 // (kPair; st2 with its alignment test) -- see sstage.
 template <class T, class = void>
@@ -79,8 +86,15 @@ __device__ __forceinline__ void sstage(const float2* stw, const Ld& ld, const St
   }
   float2 x[Q];
   if (act) {
+    if constexpr (!VFAST && has_ld_at<Ld>::value) {
+      static_for<Q>([&](auto rc) {
+        constexpr int r = decltype(rc)::value;
+        x[r] = ld.template ld_at<r, LR>(v, j);
+      });
+    } else {
 #pragma unroll
-    for (int r = 0; r < Q; ++r) x[r] = ld.ld(v, j + r * LR);
+      for (int r = 0; r < Q; ++r) x[r] = ld.ld(v, j + r * LR);
+    }
   }
   if (SYNC_MID) __syncthreads();
   if (act) {
@@ -184,8 +198,15 @@ __device__ __forceinline__ void sfft2_rows(const float2* stw, float2* tile, cons
     const int j = b - v * Q1;
     float2 x[Q0];
     if (act) {
+      if constexpr (has_ld_at<Ld0>::value) {
+        static_for<Q0>([&](auto rc) {
+          constexpr int r = decltype(rc)::value;
+          x[r] = ld0.template ld_at<r, Q1>(v, j);
+        });
+      } else {
 #pragma unroll
-      for (int r = 0; r < Q0; ++r) x[r] = ld0.ld(v, j + r * Q1);
+        for (int r = 0; r < Q0; ++r) x[r] = ld0.ld(v, j + r * Q1);
+      }
     }
     if (Ld0::kSmem) __syncthreads();
     if (act) {
