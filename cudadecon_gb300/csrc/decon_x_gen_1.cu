@@ -21,7 +21,7 @@ int xgen_fwd_1(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX384, 4, false, false, 0, 16, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX384, 4>(), st);
     case 500:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX500, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX500, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_fwd_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX648, 4>(), st);
@@ -52,7 +52,7 @@ int xgen_ratio_1(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX384, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX384, 4>(), st);
     case 500:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX500, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX500, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_ratio_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX648, 4>(), st);
@@ -83,7 +83,7 @@ int xgen_update_1(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX384, 4, false, false, 0, 16, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX384, 4>(), st);
     case 500:
       *done = true;
-      return x_update_go<StaticRunner<SPX500, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX500, 4>(), st);
+      return x_update_go<StaticRunner<SPX500, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX500, 2>(), st);
     case 648:
       *done = true;
       return x_update_go<StaticRunner<SPX648, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX648, 4>(), st);

@@ -21,7 +21,7 @@ int xgen_fwd_10(const Geom& g, const FftLen& fx, const float* X, float* Xm1, con
       return x_fwd_go<StaticRunner<SPX480, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX480, 4>(), st);
     case 625:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX625, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX625, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX625, 4>(), st);
     case 768:
       *done = true;
       return x_fwd_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX768, 2>(), st);
@@ -49,7 +49,7 @@ int xgen_ratio_10(const Geom& g, const FftLen& fx, float2* S, const float* raw, 
       return x_ratio_go<StaticRunner<SPX480, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX480, 4>(), st);
     case 625:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX625, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX625, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX625, 4>(), st);
     case 768:
       *done = true;
       return x_ratio_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX768, 2>(), st);
@@ -77,7 +77,7 @@ int xgen_update_10(const Geom& g, const FftLen& fx, const float2* S, const float
       return x_update_go<StaticRunner<SPX480, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX480, 4>(), st);
     case 625:
       *done = true;
-      return x_update_go<StaticRunner<SPX625, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX625, 2>(), st);
+      return x_update_go<StaticRunner<SPX625, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX625, 4>(), st);
     case 768:
       *done = true;
       return x_update_go<StaticRunner<SPX768, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX768, 2>(), st);

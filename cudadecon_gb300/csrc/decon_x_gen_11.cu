@@ -15,7 +15,7 @@ int xgen_fwd_11(const Geom& g, const FftLen& fx, const float* X, float* Xm1, con
       return x_fwd_go<StaticRunner<SPX270, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX270, 4>(), st);
     case 375:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX375, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX375, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX375, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX375, 8>(), st);
     case 486:
       *done = true;
       return x_fwd_go<StaticRunner<SPX486, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX486, 4>(), st);
@@ -43,7 +43,7 @@ int xgen_ratio_11(const Geom& g, const FftLen& fx, float2* S, const float* raw, 
       return x_ratio_go<StaticRunner<SPX270, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX270, 4>(), st);
     case 375:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX375, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX375, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX375, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX375, 8>(), st);
     case 486:
       *done = true;
       return x_ratio_go<StaticRunner<SPX486, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX486, 4>(), st);
@@ -71,7 +71,7 @@ int xgen_update_11(const Geom& g, const FftLen& fx, const float2* S, const float
       return x_update_go<StaticRunner<SPX270, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX270, 4>(), st);
     case 375:
       *done = true;
-      return x_update_go<StaticRunner<SPX375, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX375, 4>(), st);
+      return x_update_go<StaticRunner<SPX375, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX375, 8>(), st);
     case 486:
       *done = true;
       return x_update_go<StaticRunner<SPX486, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX486, 4>(), st);

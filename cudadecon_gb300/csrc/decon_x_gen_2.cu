@@ -24,7 +24,7 @@ int xgen_fwd_2(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX672, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX672, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX672, 4>(), st);
     case 840:
       *done = true;
       return x_fwd_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX840, 2>(), st);
@@ -52,7 +52,7 @@ int xgen_ratio_2(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX672, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX672, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX672, 4>(), st);
     case 840:
       *done = true;
       return x_ratio_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX840, 2>(), st);
@@ -80,7 +80,7 @@ int xgen_update_2(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX504, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX504, 4>(), st);
     case 672:
       *done = true;
-      return x_update_go<StaticRunner<SPX672, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX672, 2>(), st);
+      return x_update_go<StaticRunner<SPX672, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX672, 4>(), st);
     case 840:
       *done = true;
       return x_update_go<StaticRunner<SPX840, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX840, 2>(), st);

@@ -18,7 +18,7 @@ int xgen_fwd_3(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX400, 2>(), st);
+      return x_fwd_go<StaticRunner<SPX400, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX400, 4>(), st);
     case 525:
       *done = true;
       return x_fwd_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 2, splan_threads<SPX525, 2>(), st);
@@ -46,7 +46,7 @@ int xgen_ratio_3(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX400, 2>(), st);
+      return x_ratio_go<StaticRunner<SPX400, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX400, 4>(), st);
     case 525:
       *done = true;
       return x_ratio_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 2, splan_threads<SPX525, 2>(), st);
@@ -74,7 +74,7 @@ int xgen_update_3(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX300, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX300, 4>(), st);
     case 400:
       *done = true;
-      return x_update_go<StaticRunner<SPX400, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX400, 2>(), st);
+      return x_update_go<StaticRunner<SPX400, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX400, 4>(), st);
     case 525:
       *done = true;
       return x_update_go<StaticRunner<SPX525, 2, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 2, splan_threads<SPX525, 2>(), st);

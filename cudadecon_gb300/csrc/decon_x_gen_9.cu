@@ -12,7 +12,7 @@ int xgen_fwd_9(const Geom& g, const FftLen& fx, const float* X, float* Xm1, cons
       return x_fwd_go<StaticRunner<SPX180, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX180, 8>(), st);
     case 250:
       *done = true;
-      return x_fwd_go<StaticRunner<SPX250, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX250, 4>(), st);
+      return x_fwd_go<StaticRunner<SPX250, 8, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 8, splan_threads<SPX250, 8>(), st);
     case 350:
       *done = true;
       return x_fwd_go<StaticRunner<SPX350, 4, false, false, 0, 0, 0>>(g, fx.gxdev, X, Xm1, lam, predict, S, 4, splan_threads<SPX350, 4>(), st);
@@ -40,7 +40,7 @@ int xgen_ratio_9(const Geom& g, const FftLen& fx, float2* S, const float* raw, f
       return x_ratio_go<StaticRunner<SPX180, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX180, 8>(), st);
     case 250:
       *done = true;
-      return x_ratio_go<StaticRunner<SPX250, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX250, 4>(), st);
+      return x_ratio_go<StaticRunner<SPX250, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 8, splan_threads<SPX250, 8>(), st);
     case 350:
       *done = true;
       return x_ratio_go<StaticRunner<SPX350, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, raw, eps, 4, splan_threads<SPX350, 4>(), st);
@@ -68,7 +68,7 @@ int xgen_update_9(const Geom& g, const FftLen& fx, const float2* S, const float*
       return x_update_go<StaticRunner<SPX180, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX180, 8>(), st);
     case 250:
       *done = true;
-      return x_update_go<StaticRunner<SPX250, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX250, 4>(), st);
+      return x_update_go<StaticRunner<SPX250, 8, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 8, splan_threads<SPX250, 8>(), st);
     case 350:
       *done = true;
       return x_update_go<StaticRunner<SPX350, 4, false, false, 0, 0, 0>>(g, fx.gxdev, S, Y, Xout, G, dots, w, lam_next, eps, 4, splan_threads<SPX350, 4>(), st);
