@@ -107,6 +107,8 @@ def _bind(L) -> None:
         "cdx_tc_length_supported": (c_int, [c_int]),
         "cdx_tc_status": (c_int, []),
         "cdx_lambda_read": (c_int, [_F, c_int]),
+        "cdx_change_trace": (c_int, [c_int]),
+        "cdx_change_read": (c_int, [POINTER(c_double), c_int]),
         "cdx_deskew_device": (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_void_p, c_int,
                                       c_int, c_float, c_void_p]),
         "cdx_rotate_device": (c_int, [c_void_p, c_int, c_int, c_int, _F, c_void_p, c_int, c_int,

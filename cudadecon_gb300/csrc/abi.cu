@@ -137,6 +137,9 @@ struct Session {
   // acceleration factors of the last call, per iteration (cdx_lambda_trace)
   DevBuf<float> lam_hist;
   int lam_hist_n = 0;
+  // convergence norms of the last call, per iteration (cdx_change_trace)
+  DevBuf<double> chg_hist, chg_part;
+  int chg_hist_n = 0;
   cudaStream_t stream = nullptr;
   long long launches = 0;
   // acceleration-factor scratch (per-block partials and the last-block ticket)
@@ -228,6 +231,9 @@ static void release_all(Session& s) {
   s.lam.release();
   s.lam_hist.release();
   s.lam_hist_n = 0;
+  s.chg_hist.release();
+  s.chg_part.release();
+  s.chg_hist_n = 0;
   s.cc_param.release();
   s.cc_in.release();
   s.cc_out.release();
@@ -373,7 +379,8 @@ struct LoopBufs {
 
 static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t st, bool prof,
                    float** final_x, long long* launches, float* lam_hist = nullptr,
-                   int hist_n = 0) {
+                   int hist_n = 0, double* chg_hist = nullptr, int chg_n = 0,
+                   double* chg_part = nullptr) {
   const Geom& g = p.g;
   RLWork w;
   w.partials = b.partials;
@@ -425,6 +432,11 @@ static int rl_loop(const GridPlan& p, const LoopBufs& b, int nIter, cudaStream_t
     float* t = X;
     X = Xm1;
     Xm1 = t;
+    // trace: X holds X_{k+1} and Xm1 X_k until the next forward pass
+    if (chg_hist && k < chg_n) {
+      if ((rc = launch_change_norm(X, Xm1, g.nvox(), chg_part, chg_hist + k, st))) return rc;
+      *launches += 2;
+    }
   }
   *final_x = X;
   return 0;
@@ -438,8 +450,13 @@ static int rl_iterations(Session& s, int nIter, float** final_x) {
     CDX_CHECK(cudaMemsetAsync(s.lam_hist.p, 0, sizeof(float) * s.lam_hist_n, s.stream));
     hist = s.lam_hist.p;
   }
+  double* chg = nullptr;
+  if (s.chg_hist_n > 0 && s.chg_hist.p && s.chg_part.p) {
+    CDX_CHECK(cudaMemsetAsync(s.chg_hist.p, 0, sizeof(double) * s.chg_hist_n, s.stream));
+    chg = s.chg_hist.p;
+  }
   return rl_loop(s.plan, b, nIter, s.stream, g_prof.on, final_x, &s.launches, hist,
-                 s.lam_hist_n);
+                 s.lam_hist_n, chg, s.chg_hist_n, s.chg_part.p);
 }
 
 struct RLArgs {
@@ -1269,6 +1286,39 @@ int cdx_lambda_trace(int n) {
   if (s.lam_hist.ensure((size_t)n)) return 0;
   s.lam_hist_n = n;
   return 1;
+}
+
+int cdx_change_trace(int n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (n <= 0) {
+    s.chg_hist.release();
+    s.chg_part.release();
+    s.chg_hist_n = 0;
+    return 1;
+  }
+  if (s.chg_hist.ensure((size_t)n) || s.chg_part.ensure(2 * (size_t)kChangeBlocks)) return 0;
+  s.chg_hist_n = n;
+  return 1;
+}
+
+int cdx_change_read(double* out, int n) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Session& s = g_s;
+  if (!out || s.chg_hist_n <= 0 || !s.chg_hist.p) {
+    set_error("cdx_change_read", "no trace enabled (cdx_change_trace)");
+    return -1;
+  }
+  const int m = n < s.chg_hist_n ? n : s.chg_hist_n;
+  // the traced call may have run on a caller's stream (cdx_RL_device)
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemcpy(out, s.chg_hist.p, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_cuda_error("cdx_change_read", e);
+    return -1;
+  }
+  return m;
 }
 
 int cdx_lambda_read(float* out, int n) {

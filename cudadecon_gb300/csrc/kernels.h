@@ -123,6 +123,11 @@ int launch_x_inv_update(const Geom& g, const FftLen& fx, const float2* S, const 
                         cudaStream_t st);
 // The next acceleration factor from nblk float-float partials (one block).
 int launch_lambda(const float4* partials, int nblk, float* lam_next, float eps, cudaStream_t st);
+// Convergence norm of an RL step, in FP64: *out = ||x_new - x_old|| / ||x_old||
+// (0 when x_old is 0).  part: kChangeBlocks * 2 doubles of scratch.
+constexpr int kChangeBlocks = 304;
+int launch_change_norm(const float* x_new, const float* x_old, long long n, double* part,
+                       double* out, cudaStream_t st);
 // The x passes in the mixed-precision form (same contracts as the three
 // launchers above; err: the plan's error word).
 int launch_xtc_fwd(const Geom& g, const TcTables& t, const float* X, float* Xm1, const float* lam,

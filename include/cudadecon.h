@@ -160,6 +160,17 @@ int cdx_tc_status(void);
 int cdx_lambda_trace(int n);
 int cdx_lambda_read(float* out, int n);
 
+/* Convergence norms (extension; the reference computes none): with
+ * cdx_change_trace(n), n > 0, the next RL_interface / cdx_RL_device calls
+ * record after each iteration k < n the relative change of the estimate,
+ * ||X_{k+1} - X_k||_2 / ||X_k||_2, with the squares summed in FP64 by two
+ * extra kernels (none run without the trace); n <= 0 turns the trace off.
+ * cdx_change_read waits for the device and copies min(n, traced) values;
+ * returns that count, or -1 without a trace.  Returns of cdx_change_trace:
+ * 1, or 0 when its buffers cannot be allocated. */
+int cdx_change_trace(int n);
+int cdx_change_read(double* out, int n);
+
 /* Deskew / rotate / camcor on device pointers (same arithmetic as the
  * reference kernels).  rot is a host pointer to the 4 rotation-matrix floats. */
 int cdx_deskew_device(const float* in, int nx, int ny, int nz, double deskewFactor, float* out,

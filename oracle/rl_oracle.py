@@ -340,12 +340,15 @@ def zblend(img, nZblend):
 
 
 # ---------------------------------------------------------------- RL
-def rl_iterations(X0, raw, H, n_iters, dtype=np.float32, workers=None, lambdas=None):
+def rl_iterations(X0, raw, H, n_iters, dtype=np.float32, workers=None, lambdas=None,
+                  norms=None):
     """The hot loop of RichardsonLucy_GPU (RL-Biggs-Andrews.cpp:282-367).
 
     X0, raw: (nz, ny, nx) arrays; H: the OTF on the half-spectrum grid.
     Returns the final estimate.  When lambdas is a list, the acceleration
-    factor of each iteration k > 1 is appended to it."""
+    factor of each iteration k > 1 is appended to it.  When norms is a list,
+    the relative change of each iteration, ||X_{k+1} - X_k|| / ||X_k||
+    (float64 sums; the reference computes none), is appended to it."""
     ft = np.dtype(dtype).type
     workers = workers or os.cpu_count()
     shape = X0.shape
@@ -389,6 +392,10 @@ def rl_iterations(X0, raw, H, n_iters, dtype=np.float32, workers=None, lambdas=N
         X = (CC * Y).astype(dtype)
         X = np.where(X > 0, X, ft(0)).astype(dtype)
         G1 = (X - Y).astype(dtype)
+        if norms is not None:
+            d = X.astype(np.float64) - Xm1.astype(np.float64)
+            o = float(np.sum(Xm1.astype(np.float64) ** 2))
+            norms.append(float(np.sqrt(np.sum(d * d) / o)) if o > 0 else 0.0)
     return X
 
 

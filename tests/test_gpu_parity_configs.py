@@ -440,3 +440,49 @@ def test_rl_tuned_plan_variants_vs_reference(cdx, oracle, ref, torch_cuda, tmp_p
     e = rel_l2(mine, theirs)
     print(f"\ntuned {axis} plan ({feature}) {gz}x{gy}x{gx}, 8 it: rel L2 vs reference {e:.2e}")
     assert e < 1e-5
+
+
+def test_convergence_norm_trace_vs_oracle(cdx, oracle, torch_cuda, tmp_path):
+    """cdx_change_trace: the relative change of the estimate per iteration,
+    ||X_{k+1} - X_k|| / ||X_k|| summed in FP64 on the device, against the
+    float32 oracle's (same float32 estimates up to FFT rounding; relative
+    difference <= 1e-3 per iteration) and the FP64 oracle's (<= 1e-2); the
+    trace adds two launches per iteration and none when it is off."""
+    shape = (40, 96, 128)
+    nz, ny, nx = shape
+    raw = synth.bead_stack(shape, n_beads=60, psf_sigma_xy=1.3, psf_sigma_z=2.5, seed=77)
+    tab = synth.gaussian_otf_table(129, 64, 1.3, 2.5)
+    p = tmp_path / "otf.tif"
+    synth.write_otf(p, tab)
+    kw = dict(dr=0.104, dz=0.3, dr_psf=0.104, dz_psf=0.25)
+    cdx.rl_init(shape, p, **kw)
+    L = cdx.lib()
+    n = 12
+    cdx.rl_decon(raw, background=100.0, n_iters=n)
+    plain_launches = L.cdx_last_launch_count()
+    assert L.cdx_change_trace(n) == 1
+    try:
+        mine = cdx.rl_decon(raw, background=100.0, n_iters=n)
+        assert L.cdx_last_launch_count() == plain_launches + 2 * n
+        got = np.zeros(n, np.float64)
+        assert L.cdx_change_read(got.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n) == n
+    finally:
+        L.cdx_change_trace(0)
+    assert L.cdx_change_read(np.zeros(1).ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1) == -1
+    gz, gy, gx = cdx.decon_grid()
+    cdx.rl_cleanup()
+    st = oracle.rl_init(nx, ny, nz, kw["dr"], kw["dz"], kw["dr_psf"], kw["dz_psf"], 0.0, 0.0, 0,
+                        False, synth.otf_table_to_image(tab))
+    X0 = oracle.bgsub(raw[:gz, :gy, :gx].astype(np.float32), 100.0)
+    H = oracle.otf_on_grid(st, gx, gy, gz)
+    n32, n64 = [], []
+    oracle.rl_iterations(X0, X0, H, n, norms=n32)
+    oracle.rl_iterations(X0, X0, oracle.otf_on_grid(st, gx, gy, gz, dtype=np.float64), n,
+                         dtype=np.float64, norms=n64)
+    r32 = np.abs(got - n32) / np.array(n32)
+    r64 = np.abs(got - n64) / np.array(n64)
+    print(f"\nconvergence norms {gz}x{gy}x{gx}: first {got[0]:.4e}, last {got[-1]:.4e}; "
+          f"max rel diff vs float32 oracle {r32.max():.2e}, vs FP64 {r64.max():.2e}")
+    assert np.all(got > 0)
+    assert r32.max() < 1e-3
+    assert r64.max() < 1e-2

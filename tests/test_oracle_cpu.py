@@ -172,3 +172,23 @@ def test_torch_fp64_oracle_matches_numpy_fp64(oracle):
     b = OT.rl_iterations(raw, raw, Ht, 8, lambdas=lb, device="cpu").numpy()
     assert rel_l2(b, a) < 1e-12
     assert np.allclose(la, lb, rtol=0, atol=1e-12)
+
+
+def test_convergence_norms_are_relative_changes_of_the_estimate():
+    """rl_iterations(norms=...) records ||X_{k+1} - X_k|| / ||X_k|| per
+    iteration: the first equals the change from X0 computed directly, and
+    the list has one entry per iteration."""
+    import numpy as np
+    from oracle import rl_oracle as O
+    rng = np.random.default_rng(5)
+    shape = (8, 12, 16)
+    X0 = rng.uniform(1.0, 5.0, shape).astype(np.float32)
+    H = np.exp(-rng.uniform(0, 1, (8, 12, 9))).astype(np.complex64)
+    norms = []
+    X1 = O.rl_iterations(X0, X0, H, 1, norms=norms)
+    assert len(norms) == 1
+    want = np.linalg.norm(X1.astype(np.float64) - X0) / np.linalg.norm(X0.astype(np.float64))
+    assert abs(norms[0] - want) < 1e-12
+    norms = []
+    O.rl_iterations(X0, X0, H, 5, norms=norms)
+    assert len(norms) == 5 and all(n >= 0 for n in norms)
