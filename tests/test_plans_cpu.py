@@ -133,3 +133,18 @@ def test_select_keeps_candidate_zero_within_the_margin():
     assert sel["y"]["320"]["candidate"] == 0
     assert sel["z"]["120"]["candidate"] == 0
     json.dumps(sel)
+
+
+def test_select_ignores_a_column_left_out():
+    """A tuning column that failed to build or run contributes no times;
+    the others still decide."""
+    lens = {"x": [600], "y": [320], "z": [120]}
+    shapes = [(120, 320, 600)]
+    base = [0.07, 0.03, 0.05, 0.03, 0.11, 0.03, 0.05, 0.03, 0.10]
+    faster = list(base)
+    faster[4] = 0.08
+    cols = [T.axis_times(shapes, [base], lens), {a: {} for a in T.AXIS_PASSES},
+            T.axis_times(shapes, [faster], lens)]
+    sel = T.select(cols, G.candidates, 0.02)
+    assert sel["x"]["600"]["candidate"] == 2
+    assert "1" not in sel["x"]["600"]["ms"]
